@@ -1,0 +1,108 @@
+"""Build recipes for the test-side checkers (TEST INFRASTRUCTURE ONLY).
+
+* ``build_oracle()`` compiles ``dd_oracle.cpp`` (the CPU restatement) into
+  ``oracle/_build/liboracle.so``.
+* ``build_ref()`` compiles the reference's own kernel source, read in place from
+  a CTLIB checkout (``src/fan_ed_kernel.cu``, ``src/fan_ea_kernel.cu``,
+  ``src/para_kernel.cu``), for CPU execution through ``ref_emu/cuda_emu.h``, into
+  ``oracle/_ref/libctref.so``. Only the kernel part of each file is used (from
+  after its ``#include`` lines up to its first host wrapper); it is streamed to
+  the compiler through a pipe, so no copy of the reference source is written
+  anywhere. Two ``__shared__`` scalars that every thread writes with the same
+  value (``ang_error`` and ``dPoint0``, e.g. src/fan_ed_kernel.cu:53,50) are made
+  thread-private: the reference reads each of them and then overwrites it within
+  one barrier interval (src/fan_ed_kernel.cu:75-76 and :146), which on the GPU is
+  harmless because all warps read before any writes, but which a one-thread-at-
+  a-time execution would otherwise turn into a real read-after-write.
+
+Both use plain g++ (no cmake, no torch headers); ``-ffp-contract=off`` keeps the
+host results identical on x86-64 and aarch64.
+"""
+
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
+REF_SO = os.path.join(REF_DIR, "libctref.so")
+DEFAULT_REF_ROOT = "/root/reference"
+
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off"]
+
+
+def _stale(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources if os.path.exists(s))
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "dd_oracle.cpp")
+    if force or _stale(ORACLE_SO, [src]):
+        os.makedirs(BUILD_DIR, exist_ok=True)
+        tmp = ORACLE_SO + ".tmp"
+        subprocess.run(["g++", *CXXFLAGS, "-fopenmp", src, "-o", tmp], check=True)
+        os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+_KERNEL_FILES = (("ref_fan_ed", "fan_ed_kernel.cu"), ("ref_fan_ea", "fan_ea_kernel.cu"),
+                 ("ref_para", "para_kernel.cu"))
+_PRIVATE = (("__shared__ double ang_error;", "double ang_error;"),
+            ("__shared__ scalar_t dPoint0;", "scalar_t dPoint0;"))
+
+
+def _kernel_text(path: str) -> str:
+    with open(path, "r") as f:
+        lines = f.read().split("\n")
+    out, started = [], False
+    for ln in lines:
+        if not started:
+            if ln.startswith("#include"):
+                continue
+            started = True
+        if re.match(r"^torch::Tensor\b", ln):
+            break
+        out.append(ln)
+    text = "\n".join(out)
+    for a, b in _PRIVATE:
+        text = text.replace(a, b)
+    return text
+
+
+def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | None:
+    """Compile the reference kernels for CPU execution; None if no checkout."""
+    srcdir = os.path.join(ref_root, "src")
+    if not os.path.isdir(srcdir):
+        return None
+    deps = [os.path.join(srcdir, f) for _, f in _KERNEL_FILES]
+    deps += [os.path.join(HERE, "ref_emu", "cuda_emu.h"), os.path.join(HERE, "ref_emu", "ref_driver.inc"),
+             os.path.abspath(__file__)]
+    if not (force or _stale(REF_SO, deps)):
+        return REF_SO
+    parts = ['#include "cuda_emu.h"']
+    for ns, fname in _KERNEL_FILES:
+        parts.append(f"namespace {ns} {{")
+        parts.append(f'#line 1 "{fname}"')
+        parts.append(_kernel_text(os.path.join(srcdir, fname)))
+        parts.append(f"}}  // namespace {ns}")
+    with open(os.path.join(HERE, "ref_emu", "ref_driver.inc")) as f:
+        parts.append(f.read())
+    os.makedirs(REF_DIR, exist_ok=True)
+    tmp = REF_SO + ".tmp"
+    subprocess.run(["g++", *CXXFLAGS, "-w", "-I", os.path.join(HERE, "ref_emu"), "-x", "c++", "-",
+                    "-o", tmp], input="\n".join(parts).encode(), check=True)
+    os.replace(tmp, REF_SO)
+    return REF_SO
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_ref(force="--force" in sys.argv))
