@@ -1,0 +1,371 @@
+"""Benchmark: ray-updates/s of projection + projection_t (the autograd pair) on
+the fan equal-distance workload 16 x 512^2, 1152 views, 736 bins.
+
+One step = A x followed by A^T y for the whole batch (one launch of each
+operator for all 16 slices). A ray-update is one (slice, view, detector bin,
+image line); one step is 2 * 16 * 1152 * 736 * 512 = 1.39e10 ray-updates.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). Timing: CUDA events on the launching stream around
+each step, L2 flushed (256 MB write) before every timed step, max over ranks.
+Under torchrun each rank runs an independent replica of the workload (the
+operators need no exchange between slices): weak scaling.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "fan_ed_512"
+METRIC = "ray-updates/s proj+adjoint 512² fan-ED B=16, batched vs plain, rel-L2≤1e-5"
+UNIT = "ray-updates/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, p[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _cpu_baseline(w, seconds_target: float = 15.0) -> dict:
+    """The CPU oracle (fp32, reference promotions) on a bounded sample of the
+    workload: one slice, a contiguous subset of the views, A then A^T, all
+    host threads. Returned in ray-updates/s."""
+    import oracle
+    from ctlib_gb300.workloads import ellipse_phantom
+    s = w.slices[0]
+    o = list(s.options)
+    V, D, W, H = (int(o[i]) for i in range(4))
+    threads = oracle.max_threads()
+    img = ellipse_phantom(H, W, o[4], s.seed)[None, None]
+    nv = 16
+    while True:
+        sub = list(o)
+        sub[0] = float(nv)
+        t0 = time.perf_counter()
+        sino = oracle.run("projection", img, sub, oracle.MODE_F32, threads)
+        oracle.run("projection_t", sino, sub, oracle.MODE_F32, threads)
+        dt = time.perf_counter() - t0
+        if dt > seconds_target / 4 or nv >= V:
+            break
+        nv = min(V, int(nv * max(2.0, seconds_target / 4 / max(dt, 1e-3))))
+    reps = max(1, int(seconds_target / max(dt, 1e-3)))
+    reps = min(reps, 8)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sino = oracle.run("projection", img, sub, oracle.MODE_F32, threads)
+        oracle.run("projection_t", sino, sub, oracle.MODE_F32, threads)
+    dt = (time.perf_counter() - t0) / reps
+    ru = 2 * nv * D * max(W, H)
+    return {"value": ru / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"1 slice of {w.name}, views 0..{nv - 1} of {V}, projection + projection_t, "
+                      f"{reps} rep(s), {dt:.2f} s each"}
+
+
+def run_reference(args):
+    """Reference arm: the reference has no CPU path; its distance-driven loops
+    run as the OpenMP oracle port on the host cores."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from ctlib_gb300.workloads import WORKLOADS
+    from oracle import build as obuild
+    obuild.build_oracle()
+    w = WORKLOADS[args.workload]()
+    cb = _cpu_baseline(w, seconds_target=max(5.0, 20.0 / max(1, args.steps)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic ellipse phantoms",
+            "config": {"workload": w.name, "global_batch": len(w.slices), "cpu_sample": cb["sample"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _fp32_peak(device) -> dict:
+    """Measured FFMA throughput of this GPU (lane-FMAs/s) from a short
+    register-resident FMA kernel in libctgb (see csrc/peak_fp32.cu)."""
+    from ctlib_gb300 import _peak
+    return _peak.measure(device)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import ctlib_gb300 as ctlib
+    from ctlib_gb300 import autograd as ag
+    from ctlib_gb300.workloads import WORKLOADS, phantoms
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]()
+    B = len(w.slices)
+    opts = torch.tensor(w.slices[0].options, dtype=torch.float32)
+    V, D, W, H = (int(w.slices[0].options[i]) for i in range(4))
+    img_h = torch.from_numpy(np.stack(phantoms(w))[:, None]).contiguous()
+    img = img_h.to(dev)
+    ru_step = 2 * w.ray_updates()
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        s = ctlib.projection(img, opts)
+        return ctlib.projection_t(s, opts)
+
+    plan = ctlib.get_plan(opts, torch.float32, dev)
+    # warm-up (builds plans, workspace, caches)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # -- device-resident timing, per-op events -----------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(local)
+    clk.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e0, e1, e2 = ev[i]
+        e0.record(stream)
+        s = ctlib.projection(img, opts)
+        e1.record(stream)
+        ctlib.projection_t(s, opts)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    t_a = [ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)]
+    t_at = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
+    step_ms = sum(a + b for a, b in zip(t_a, t_at)) / args.steps
+    if ws > 1:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = ws * ru_step / (step_ms / 1e3)
+
+    # -- plain per-slice path (one call per slice) ---------------------------
+    torch.cuda.synchronize()
+    plain_ms = []
+    for i in range(max(2, args.steps // 2)):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for k in range(B):
+            s = ctlib.projection(img[k:k + 1], opts)
+            ctlib.projection_t(s, opts)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(a.elapsed_time(b))
+    plain_value = ru_step / (statistics.median(plain_ms) / 1e3)
+
+    # -- end to end through the autograd API with host buffers ---------------
+    y_meas = ctlib.projection(img, opts)
+    img_pin = img_h.pin_memory()
+    grad_h = torch.empty_like(img_h).pin_memory()
+    loss_h = torch.empty((), dtype=torch.float32).pin_memory()
+    op = ag.Projector(opts)
+
+    def e2e_step():
+        x = img_pin.to(dev, non_blocking=True).requires_grad_(True)
+        r = op(x) - y_meas
+        loss = 0.5 * (r * r).sum()
+        loss.backward()
+        grad_h.copy_(x.grad, non_blocking=True)
+        loss_h.copy_(loss.detach(), non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_mean = sum(e2e_ms) / len(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e_mean], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_mean = float(t.item())
+    e2e_value = ws * ru_step / (e2e_mean / 1e3)
+
+    # -- parity of the timed operator pair vs the FP64 oracle (1 slice) -------
+    parity = None
+    if rank == 0:
+        import oracle
+        x0 = img_h[:1].numpy()
+        a_ref = oracle.run("projection", x0, w.slices[0].options, oracle.MODE_F64_ON_F32)
+        a_got = ctlib.projection(img[:1], opts).cpu().numpy()
+        at_ref = oracle.run("projection_t", a_got, w.slices[0].options, oracle.MODE_F64_ON_F32)
+        at_got = ctlib.projection_t(torch.from_numpy(a_got).to(dev), opts).cpu().numpy()
+        parity = {"projection_rel_l2_vs_fp64": oracle.rel_l2(a_got, a_ref),
+                  "projection_t_rel_l2_vs_fp64": oracle.rel_l2(at_got, at_ref)}
+
+    # -- roofline of the dominant kernel -------------------------------------
+    ta, tat = statistics.mean(t_a), statistics.mean(t_at)
+    dom = "det_gather (projection)" if ta >= tat else "pix_gather (projection_t)"
+    dom_ms = max(ta, tat)
+    # algorithmic bytes of one launch: read input + write output once
+    alg_bytes = (B * H * W + B * V * D) * 4
+    hbm_peak = _measured("hbm_gbs", 6790.7)
+    achieved_gbs = alg_bytes / (dom_ms / 1e3) / 1e9
+    peak = _fp32_peak(dev) if rank == 0 else None
+    roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak[0], "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(), "peak_source": hbm_peak[1],
+            "kernel": dom, "kernel_ms": dom_ms, "algorithmic_bytes": alg_bytes}
+    roof_fp32 = None
+    if peak:
+        # survey model: 8 FP32 lane-ops per ray-update at the measured FFMA rate
+        model_peak = peak["lane_ops_per_s"] / 8.0
+        ru_dom = w.ray_updates()
+        ach = ru_dom / (dom_ms / 1e3)
+        roof_fp32 = {"achieved": ach, "peak": model_peak, "unit": "ray-updates/s", "frac": ach / model_peak,
+                     "model": "8 FP32 lane-ops per ray-update at measured FFMA lane-op rate",
+                     "measured_fp32": peak}
+
+    if rank == 0:
+        cb = _cpu_baseline(w)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic ellipse phantoms (seeded)",
+                "config": {"workload": w.name, "global_batch": B * ws, "per_gpu_batch": B, "views": V,
+                           "dets": D, "image": [H, W], "parallelism": f"replicas{ws}",
+                           "l2": "flushed (256 MB write) before every timed step",
+                           "ray_updates_per_step": ru_step},
+                "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": statistics.median(plain_ms),
+                          "note": "one projection + projection_t call per slice"},
+                "batched_over_plain": value / ws / plain_value,
+                "ms_projection": ta, "ms_projection_t": tat,
+                "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_mean,
+                        "h2d_bytes_per_step": int(img_h.numel() * 4),
+                        "d2h_bytes_per_step": int(img_h.numel() * 4 + 4),
+                        "path": "ctlib_gb300.autograd.Projector: H2D image, A, loss, backward (A^T), D2H grad+loss"},
+                "gpu_launches": 4 * args.steps,
+                "clocks": clocks, "roofline": roof, "roofline_fp32": roof_fp32, "parity": parity,
+                "cpu_baseline": cb}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def _measured(key, fallback):
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)[key]), "measured"
+    except (OSError, KeyError, ValueError):
+        return fallback, "fallback"
+
+
+def _ncu_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary, if one exists (profiles/*.json written from an ncu capture)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    args = ap.parse_args()
+    if args.warmup < 1:
+        args.warmup = 1
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

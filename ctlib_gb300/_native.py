@@ -1,0 +1,117 @@
+"""Build and load ``libctgb.so`` (the sm_103a kernels behind include/ctgb.h).
+
+The library is compiled in-tree with nvcc (``build()``); ``lib()`` loads it with
+ctypes. There is no fallback: if the library is missing or fails to load, every
+operator raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import shutil
+import subprocess
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD_DIR = os.path.join(PKG, "_build")
+SO_PATH = os.path.join(BUILD_DIR, "libctgb.so")
+INCLUDE = os.path.join(ROOT, "include")
+SOURCES = [os.path.join(CSRC, "ctgb_kernels.cu"), os.path.join(CSRC, "geometry.cpp")]
+HEADERS = [os.path.join(INCLUDE, "ctgb.h"), os.path.join(CSRC, "geometry.h")]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+OK, ERR_INVALID, ERR_CUDA, ERR_WORKSPACE = 0, 1, 2, 3
+OP_PROJECTION, OP_PROJECTION_T, OP_BACKPROJECTION, OP_BACKPROJECTION_T, OP_FBP = 0, 1, 2, 3, 4
+
+_lock = threading.Lock()
+_lib = None
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found; set NVCC or put the CUDA toolkit on PATH")
+
+
+def _stale() -> bool:
+    if not os.path.exists(SO_PATH):
+        return True
+    t = os.path.getmtime(SO_PATH)
+    return any(os.path.getmtime(p) > t for p in SOURCES + HEADERS)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile libctgb.so for sm_103a (no-op when up to date)."""
+    if not force and not _stale():
+        return SO_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = SO_PATH + ".tmp"
+    cmd = [nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++17", "-I", INCLUDE, "-Xcompiler", "-fPIC", "-shared",
+           *SOURCES, "-o", tmp]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, SO_PATH)
+    return SO_PATH
+
+
+def _declare(l):
+    c_int, c_size, vp = ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p
+    dptr = ctypes.POINTER(ctypes.c_double)
+    l.ctgb_plan_create.argtypes = [ctypes.POINTER(vp), dptr, c_int, c_int, c_int]
+    l.ctgb_plan_create.restype = c_int
+    l.ctgb_plan_destroy.argtypes = [vp]
+    l.ctgb_plan_destroy.restype = c_int
+    ip = ctypes.POINTER(c_int)
+    l.ctgb_plan_info.argtypes = [vp, ip, ip, ip, ip, ip, ip]
+    l.ctgb_plan_info.restype = c_int
+    l.ctgb_workspace_size.argtypes = [vp, c_int, c_int]
+    l.ctgb_workspace_size.restype = c_size
+    for name in ("ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
+                 "ctgb_fbp"):
+        f = getattr(l, name)
+        f.argtypes = [vp, vp, vp, c_int, vp, c_size, vp]
+        f.restype = c_int
+    l.ctgb_last_error.argtypes = []
+    l.ctgb_last_error.restype = ctypes.c_char_p
+    l.ctgb_version.restype = c_int
+    l.ctgb_geometry_query.argtypes = [dptr, c_int, c_int, c_int, dptr, c_size]
+    l.ctgb_geometry_query.restype = ctypes.c_long
+    return l
+
+
+def lib():
+    """The loaded library; raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(SO_PATH):
+                    raise RuntimeError(
+                        f"ctlib_gb300 native library not built ({SO_PATH} missing); "
+                        "run `python -c 'import __graft_entry__ as g; g.build()'`")
+                _lib = _declare(ctypes.CDLL(SO_PATH))
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().ctgb_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int, what: str):
+    if rc == OK:
+        return
+    msg = f"{what}: {last_error()}"
+    if rc == ERR_INVALID:
+        raise ValueError(msg)
+    raise RuntimeError(msg)
+
+
+EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_workspace_size",
+            "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
+            "ctgb_fbp", "ctgb_last_error", "ctgb_version", "ctgb_geometry_query")

@@ -1,0 +1,212 @@
+// Host-side scan geometry (see geometry.h). Expressions that the reference
+// evaluates in scalar_t are evaluated in T here, those it evaluates in double
+// are evaluated in double, so the rounded boundaries match the reference's.
+#include "geometry.h"
+
+#include <cmath>
+#include <limits>
+
+namespace ctgb {
+
+namespace {
+
+template <class T> inline T map_x(T sx, T sy, T dx, T dy) { return (sx * dy - sy * dx) / (dy - sy); }
+template <class T> inline T map_y(T sx, T sy, T dx, T dy) { return (sy * dx - sx * dy) / (dx - sx); }
+
+template <class T>
+bool build(const double* o, int n, HostGeom& g, std::string& err) {
+  if (n < 9) { err = "options vector needs at least 9 entries"; return false; }
+  const double st = o[n - 1];
+  if (!(st == 0.0 || st == 1.0 || st == 2.0)) { err = "scan_type (last option) must be 0, 1 or 2"; return false; }
+  g.scan = (int)st;
+  if (g.scan != kPara && n < 12) { err = "fan-beam options vector needs 12 entries"; return false; }
+  for (int i = 0; i < 4; ++i) {
+    if (!(o[i] >= 1.0) || o[i] != std::floor(o[i]) || o[i] > 65536.0) {
+      err = "views, dets, width and height must be positive integers";
+      return false;
+    }
+  }
+  const T views = (T)o[0], dets = (T)o[1], width = (T)o[2], height = (T)o[3];
+  const T dImg = (T)o[4], dDet = (T)o[5], Ang0 = (T)o[6], dAng = (T)o[7];
+  T s2r = 0, d2r = 0, binshift;
+  if (g.scan == kPara) {
+    binshift = (T)o[8];
+  } else {
+    s2r = (T)o[8]; d2r = (T)o[9]; binshift = (T)o[10];
+  }
+  if (!(dImg > 0) || !(dDet > 0)) { err = "dImg and dDet must be positive"; return false; }
+  if (g.scan != kPara && !(s2r > 0 && s2r + d2r > 0)) { err = "s2r must be positive"; return false; }
+  g.V = (int)o[0]; g.D = (int)o[1]; g.W = (int)o[2]; g.H = (int)o[3];
+  g.L = g.H > g.W ? g.H : g.W;
+  g.views = views; g.dets = dets; g.width = width; g.height = height; g.dImg = dImg; g.dDet = dDet;
+  g.Ang0 = Ang0; g.dAng = dAng; g.s2r = s2r; g.d2r = d2r; g.binshift = binshift;
+  const int V = g.V, D = g.D, L = g.L;
+  g.flags.assign(V, 0);
+  g.src.assign((size_t)V * 2, 0.0);
+  g.db.assign((size_t)V * (D + 1), 0.0);
+  g.fq.assign((size_t)V * D, 0.0);
+  g.fbt.assign((size_t)V * D, 1.0);
+  g.lp.assign((size_t)V * L * 4, 0.0);
+  g.inv.assign((size_t)V * 5, 0.0);
+
+  const double PI = std::acos(-1.0);
+  const T x0 = -width / 2 * dImg;   // src/fan_ed_kernel.cu:107
+  const T y0 = -height / 2 * dImg;  // src/fan_ed_kernel.cu:196
+  g.x0 = x0; g.y0 = y0;
+  // virtual detector pitch/shift: scalar_t expressions widened to double (:68-69)
+  const double virdDet = (double)(s2r / (s2r + d2r) * dDet);
+  const double virshift = (double)(s2r / (s2r + d2r) * binshift);
+  const double R = (double)s2r;
+  double max_half_x = std::fabs((double)x0), max_half_y = std::fabs((double)y0);
+
+  std::vector<T> dbT(D + 1), cosb(D + 1);
+  for (int v = 0; v < V; ++v) {
+    const double ang = (double)((T)v * dAng + Ang0);  // src/fan_ed_kernel.cu:61
+    const bool xb = std::fabs(ang - std::round(ang / PI) * PI) * 4 / PI <= 1;
+    const double e2 = (ang - std::floor(ang / 2 / PI) * 2 * PI) * 4 / PI;
+    const bool flip = e2 >= 3 && e2 < 7;
+    const double c = std::cos(ang), s = std::sin(ang);
+    g.flags[v] = (xb ? 1 : 0) | (flip ? 2 : 0);
+    const T sx = (T)(-s * (double)s2r), sy = (T)(c * (double)s2r);
+    g.src[2 * v] = sx; g.src[2 * v + 1] = sy;
+    if (g.scan != kPara) {
+      // the source must stay outside the image along the integration lines
+      if ((xb && std::fabs((double)sy) <= max_half_y) || (!xb && std::fabs((double)sx) <= max_half_x)) {
+        err = "source lies inside the image field of view";
+        return false;
+      }
+    }
+    const double e = flip ? -1.0 : 1.0;
+    for (int b = 0; b <= D; ++b) {
+      const T tb = flip ? (dets / 2 - (T)b) : ((T)b - dets / 2);
+      T val;
+      if (g.scan == kFanED) {
+        const double sdet = (double)tb * virdDet + virshift;
+        const T detx = (T)(sdet * c), dety = (T)(sdet * s);
+        val = xb ? map_x(sx, sy, detx, dety) : map_y(sx, sy, detx, dety);
+      } else if (g.scan == kFanEA) {
+        const double beta = (double)(tb * dDet + binshift) + ang;
+        val = xb ? (T)((double)sx + std::sin(beta) / std::cos(beta) * (double)sy)
+                 : (T)((double)sy + std::cos(beta) / std::sin(beta) * (double)sx);
+      } else {
+        const T num = tb * dDet + binshift;
+        val = (T)((double)num / (xb ? c : s));
+      }
+      dbT[b] = val;
+      g.db[(size_t)v * (D + 1) + b] = (double)val;
+    }
+    for (int b = 0; b < D; ++b) {
+      if (!(dbT[b + 1] > dbT[b])) {
+        err = "detector boundaries are not strictly increasing on the projection axis";
+        return false;
+      }
+    }
+    if (g.scan != kPara) {
+      for (int b = 0; b <= D; ++b) {
+        const T u = dbT[b];
+        cosb[b] = xb ? std::fabs(sy) / std::sqrt((u - sx) * (u - sx) + sy * sy)
+                     : std::fabs(sx) / std::sqrt((u - sy) * (u - sy) + sx * sx);
+      }
+      for (int d = 0; d < D; ++d) {
+        const T cbar = (cosb[d + 1] + cosb[d]) / 2;
+        const T w = dbT[d + 1] - dbT[d];
+        g.fq[(size_t)v * D + d] = (double)dImg / ((double)cbar * (double)w);
+        if (g.scan == kFanEA) g.fbt[(size_t)v * D + d] = (double)dImg / (double)cbar;
+      }
+    } else {
+      const T dinterval = dImg / dDet;
+      for (int d = 0; d < D; ++d) g.fq[(size_t)v * D + d] = (double)dinterval;
+    }
+    // per-line affine pixel-edge maps
+    const int nl = xb ? g.H : g.W;
+    for (int l = 0; l < nl; ++l) {
+      double alpha, sigma;
+      if (xb) {
+        const T i0y = (T)(((double)(height / 2 - (T)l) - 0.5) * (double)dImg);
+        if (g.scan != kPara) {
+          const double den = (double)i0y - (double)sy;
+          alpha = ((double)sx * (double)i0y - (double)sy * (double)x0) / den;
+          sigma = -(double)sy * (double)dImg / den;
+        } else {
+          alpha = s / c * (double)i0y + (double)x0;
+          sigma = (double)dImg;
+        }
+      } else {
+        const T i0x = (T)(((double)((T)l - width / 2) + 0.5) * (double)dImg);
+        if (g.scan != kPara) {
+          const double den = (double)i0x - (double)sx;
+          alpha = ((double)sy * (double)i0x - (double)sx * (double)y0) / den;
+          sigma = -(double)sx * (double)dImg / den;
+        } else {
+          alpha = (double)y0 + c / s * (double)i0x;
+          sigma = (double)dImg;
+        }
+      }
+      if (!(sigma > 0)) { err = "degenerate pixel projection (source inside the image?)"; return false; }
+      double* q = &g.lp[((size_t)v * L + l) * 4];
+      q[0] = alpha; q[1] = sigma; q[2] = -alpha / sigma; q[3] = 1.0 / sigma;
+    }
+    // inverse boundary map seed
+    double* P = &g.inv[(size_t)v * 5];
+    if (g.scan == kPara) {
+      P[0] = xb ? c : s; P[1] = 1.0; P[2] = 0.0;
+      P[3] = D / 2.0 - e * (double)binshift / (double)dDet;
+      P[4] = e / (double)dDet;
+    } else {
+      P[0] = xb ? c : s; P[1] = R; P[2] = xb ? s : -c;
+      if (g.scan == kFanED) {
+        P[3] = D / 2.0 - e * virshift / virdDet;
+        P[4] = e * R / virdDet;
+      } else {
+        P[3] = D / 2.0 - e * (double)binshift / (double)dDet;
+        P[4] = e / (double)dDet;
+      }
+    }
+  }
+
+  // FBP detector pre-weight and ramp taps (src/fan_ed_kernel.cu:1349-1366,
+  // src/fan_ea_kernel.cu:1075-1090, src/para_kernel.cu:823-833)
+  g.wpre.assign(D, 1.0);
+  T dfilt = dDet;
+  if (g.scan == kFanED) {
+    const T vd = dDet * s2r / (s2r + d2r);
+    for (int k = 0; k < D; ++k) {
+      T t = (-dets / 2 + (T)0.5) + (T)k;
+      T r = t * vd;
+      r = r * r;
+      g.wpre[k] = (double)(s2r / std::sqrt(s2r * s2r + r));
+    }
+    dfilt = vd;
+    g.wscale = (double)vd;
+  } else if (g.scan == kFanEA) {
+    for (int k = 0; k < D; ++k) {
+      T t = (-dets / 2 + (T)0.5) + (T)k;
+      T r = std::cos(t * dDet);
+      g.wpre[k] = (double)(r * s2r * dDet);
+    }
+  } else {
+    for (int k = 0; k < D; ++k) g.wpre[k] = (double)dDet;
+  }
+  g.taps.assign(2 * D - 1, 0.0);
+  for (int j = 0; j < 2 * D - 1; ++j) {
+    const int x = j - D + 1;
+    if (std::abs(x) % 2 == 1)
+      g.taps[j] = (double)(T)(-1 / (PI * PI * x * x * (double)dfilt * (double)dfilt));
+    else if (x == 0)
+      g.taps[j] = (double)(T)(1 / (4 * dfilt * dfilt));
+  }
+  return true;
+}
+
+}  // namespace
+
+bool build_geometry(const double* options, int n_options, int dtype, HostGeom& g, std::string& err) {
+  g = HostGeom();
+  g.dtype = dtype;
+  if (dtype == 0) return build<float>(options, n_options, g, err);
+  if (dtype == 1) return build<double>(options, n_options, g, err);
+  err = "dtype must be 0 (float32) or 1 (float64)";
+  return false;
+}
+
+}  // namespace ctgb

@@ -1,0 +1,194 @@
+"""Drop-in replacements for the functions of CTLIB's ``ctlib`` module.
+
+``projection``, ``projection_t``, ``backprojection``, ``backprojection_t`` and
+``fbp`` take and return the same tensors as the reference (src/ctlib.cpp:15-99):
+images ``B x 1 x H x W``, sinograms ``B x 1 x V x D``, contiguous CUDA tensors
+in float32 or float64, and the reference's options vector. Each call returns a
+fresh tensor on the input's device and launches on the current CUDA stream.
+
+Differences from the reference, all on error paths or convenience:
+* the options vector may live on the CPU or the GPU, in any float dtype (its
+  values are rounded to the data dtype, which is what the reference reads);
+  a GPU options tensor is read once per (tensor, version), not on every call;
+* an unknown scan_type, mismatched shapes or non-CUDA / non-contiguous inputs
+  raise ``ValueError`` / ``RuntimeError`` instead of terminating the process
+  (src/ctlib.cpp:26) or reading out of bounds;
+* inputs with C > 1 channels use channel 0, as the reference does.
+"""
+
+from __future__ import annotations
+
+import threading
+from collections import OrderedDict
+
+import torch
+
+from . import _native as N
+
+_FLOATS = (torch.float32, torch.float64)
+
+
+class Plan:
+    """Geometry of one options vector on one device, uploaded once."""
+
+    def __init__(self, values: tuple, dtype: torch.dtype, device: int):
+        import ctypes
+        self.values = values
+        self.dtype = dtype
+        self.device = device
+        arr = (ctypes.c_double * len(values))(*values)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(device):
+            rc = N.lib().ctgb_plan_create(ctypes.byref(h), arr, len(values),
+                                          0 if dtype == torch.float32 else 1, device)
+        N.check(rc, "options")
+        self.handle = h
+        vals = [ctypes.c_int() for _ in range(6)]
+        N.lib().ctgb_plan_info(h, *[ctypes.byref(x) for x in vals])
+        self.views, self.dets, self.width, self.height, self.scan_type, _ = (x.value for x in vals)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            try:
+                N._lib.ctgb_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def workspace_bytes(self, op: int, batch: int) -> int:
+        return int(N.lib().ctgb_workspace_size(self.handle, op, batch))
+
+    def run(self, op: int, x: torch.Tensor, out: torch.Tensor, stream=None) -> torch.Tensor:
+        """Launch ``op`` on contiguous device tensors (no checks beyond the C side)."""
+        batch = x.shape[0]
+        nbytes = self.workspace_bytes(op, batch)
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device)
+        fn = _FN[op]
+        rc = fn(self.handle, x.data_ptr(), out.data_ptr(), batch, ws.data_ptr(), nbytes, stream.cuda_stream)
+        N.check(rc, _NAMES[op])
+        return out
+
+
+_NAMES = {N.OP_PROJECTION: "projection", N.OP_PROJECTION_T: "projection_t",
+          N.OP_BACKPROJECTION: "backprojection", N.OP_BACKPROJECTION_T: "backprojection_t", N.OP_FBP: "fbp"}
+
+
+class _FnTable(dict):
+    def __missing__(self, op):
+        l = N.lib()
+        fn = {N.OP_PROJECTION: l.ctgb_projection, N.OP_PROJECTION_T: l.ctgb_projection_t,
+              N.OP_BACKPROJECTION: l.ctgb_backprojection, N.OP_BACKPROJECTION_T: l.ctgb_backprojection_t,
+              N.OP_FBP: l.ctgb_fbp}[op]
+        self[op] = fn
+        return fn
+
+
+_FN = _FnTable()
+
+_plan_lock = threading.Lock()
+_plans: "OrderedDict[tuple, Plan]" = OrderedDict()
+_MAX_PLANS = 256
+_opt_cache: "OrderedDict[tuple, tuple]" = OrderedDict()
+
+
+def _option_values(options) -> tuple:
+    if isinstance(options, torch.Tensor):
+        key = (options.data_ptr(), options._version, str(options.device), options.numel(), options.dtype)
+        hit = _opt_cache.get(key)
+        if hit is not None:
+            return hit
+        vals = tuple(float(v) for v in options.detach().reshape(-1).tolist())
+        _opt_cache[key] = vals
+        if len(_opt_cache) > 1024:
+            _opt_cache.popitem(last=False)
+        return vals
+    return tuple(float(v) for v in options)
+
+
+def get_plan(options, dtype: torch.dtype, device) -> Plan:
+    """Cached plan for (options values, dtype, device)."""
+    dev = torch.device(device)
+    idx = dev.index if dev.index is not None else torch.cuda.current_device()
+    vals = _option_values(options)
+    key = (vals, dtype, idx)
+    with _plan_lock:
+        p = _plans.get(key)
+        if p is not None:
+            _plans.move_to_end(key)
+            return p
+    p = Plan(vals, dtype, idx)
+    with _plan_lock:
+        _plans[key] = p
+        while len(_plans) > _MAX_PLANS:
+            _plans.popitem(last=False)
+    return p
+
+
+def clear_plans():
+    with _plan_lock:
+        _plans.clear()
+        _opt_cache.clear()
+
+
+def _check_input(x: torch.Tensor, name: str) -> torch.Tensor:
+    if not isinstance(x, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if not x.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor")
+    if not x.is_contiguous():
+        raise RuntimeError(f"{name} must be contiguous")
+    if x.dtype not in _FLOATS:
+        raise RuntimeError(f"{name} must be float32 or float64, got {x.dtype}")
+    if x.dim() != 4:
+        raise ValueError(f"{name} must be 4-D (B x 1 x H x W or B x 1 x V x D), got shape {tuple(x.shape)}")
+    if x.shape[1] != 1:
+        x = x[:, :1].contiguous()
+    return x
+
+
+def _apply(op: int, x: torch.Tensor, options, name: str) -> torch.Tensor:
+    x = _check_input(x, name)
+    plan = get_plan(options, x.dtype, x.device)
+    B = x.shape[0]
+    img_shape = (plan.height, plan.width)
+    sino_shape = (plan.views, plan.dets)
+    if op in (N.OP_PROJECTION, N.OP_BACKPROJECTION_T):
+        if tuple(x.shape[2:]) != img_shape:
+            raise ValueError(f"{name}: image is {tuple(x.shape[2:])}, options give height x width {img_shape}")
+        out = torch.empty((B, 1) + sino_shape, dtype=x.dtype, device=x.device)
+    else:
+        if tuple(x.shape[2:]) != sino_shape:
+            raise ValueError(f"{name}: sinogram is {tuple(x.shape[2:])}, options give views x dets {sino_shape}")
+        out = torch.empty((B, 1) + img_shape, dtype=x.dtype, device=x.device)
+    if B == 0:
+        return out
+    with torch.cuda.device(x.device):
+        return plan.run(op, x, out)
+
+
+def projection(image: torch.Tensor, options) -> torch.Tensor:
+    """A: image B x 1 x H x W -> sinogram B x 1 x V x D (src/ctlib.cpp:56-69)."""
+    return _apply(N.OP_PROJECTION, image, options, "image")
+
+
+def projection_t(projection: torch.Tensor, options) -> torch.Tensor:
+    """A^T: sinogram -> image (src/ctlib.cpp:71-84)."""
+    return _apply(N.OP_PROJECTION_T, projection, options, "projection")
+
+
+def backprojection(projection: torch.Tensor, options) -> torch.Tensor:
+    """B, the FBP backprojector with distance weighting: sinogram -> image (src/ctlib.cpp:30-43)."""
+    return _apply(N.OP_BACKPROJECTION, projection, options, "projection")
+
+
+def backprojection_t(image: torch.Tensor, options) -> torch.Tensor:
+    """B^T: image -> sinogram (src/ctlib.cpp:15-28)."""
+    return _apply(N.OP_BACKPROJECTION_T, image, options, "image")
+
+
+def fbp(projection: torch.Tensor, options) -> torch.Tensor:
+    """RL-filtered backprojection: sinogram -> image (src/ctlib.cpp:86-99)."""
+    return _apply(N.OP_FBP, projection, options, "projection")

@@ -1,0 +1,115 @@
+/* ctgb.h - C ABI of the GB300 distance-driven CT operators (libctgb.so).
+ *
+ * Drop-in boundary for CTLIB's pybind11 module `ctlib` (src/ctlib.cpp:106-114):
+ * the five operators below replace projection / projection_t / backprojection /
+ * backprojection_t / fbp with the same tensor layouts (B x 1 x H x W images,
+ * B x 1 x V x D sinograms, contiguous, fp32 or fp64) and the same options
+ * vector semantics, but take plain device pointers, a caller-provided scratch
+ * buffer and a CUDA stream, and return a status code instead of terminating
+ * the process on a bad scan_type (src/ctlib.cpp:26).
+ *
+ * The options vector is decoded once into a plan (ctgb_plan_create) instead of
+ * on every call through blocking .item() reads of a device tensor
+ * (src/ctlib.cpp:18, src/fan_ed_kernel.cu:1165-1181).
+ *
+ * All functions are thread-safe with respect to distinct plans; one plan may
+ * be used from several threads/streams concurrently (it is read-only after
+ * creation). Errors: CTGB_OK (0) on success, otherwise a CTGB_ERR_* code and a
+ * message retrievable with ctgb_last_error() on the calling thread.
+ */
+#ifndef CTGB_H
+#define CTGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ctgb_plan ctgb_plan;
+
+enum {
+  CTGB_OK = 0,
+  CTGB_ERR_INVALID = 1,   /* bad options, sizes, pointers or dtype */
+  CTGB_ERR_CUDA = 2,      /* a CUDA runtime call or launch failed */
+  CTGB_ERR_WORKSPACE = 3  /* scratch buffer smaller than ctgb_workspace_size() */
+};
+
+enum { CTGB_FLOAT32 = 0, CTGB_FLOAT64 = 1 };
+
+enum {
+  CTGB_OP_PROJECTION = 0,
+  CTGB_OP_PROJECTION_T = 1,
+  CTGB_OP_BACKPROJECTION = 2,
+  CTGB_OP_BACKPROJECTION_T = 3,
+  CTGB_OP_FBP = 4
+};
+
+/* Decode an options vector (host array, the reference's layout: fan
+ * [views, dets, width, height, dImg, dDet, Ang0, dAng, s2r, d2r, binshift,
+ * scan_type], parallel [views, dets, width, height, dImg, dDet, Ang0, dAng,
+ * binshift, ..., scan_type]; src/fan_ed_kernel.cu:1165-1175,
+ * src/para_kernel.cu:687-695) and upload the per-view geometry tables to
+ * `device`. Replaces the option decoding of every reference host wrapper. */
+int ctgb_plan_create(ctgb_plan** plan, const double* options, int n_options, int dtype, int device);
+int ctgb_plan_destroy(ctgb_plan* plan);
+
+/* views, dets, width, height, scan_type, dtype of a plan (any may be NULL) */
+int ctgb_plan_info(const ctgb_plan* plan, int* views, int* dets, int* width, int* height,
+                   int* scan_type, int* dtype);
+
+/* Scratch bytes `op` needs for `batch` slices (0 is a valid answer). */
+size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch);
+
+/* A: image (B x 1 x H x W) -> sinogram (B x 1 x V x D).
+ * Replaces projection(): src/ctlib.cpp:56-69, prj_{fan_ed,fan_ea,para}_cuda
+ * (src/fan_ed_kernel.cu:1163-1195, src/fan_ea_kernel.cu:923-955,
+ *  src/para_kernel.cu:685-714). */
+int ctgb_projection(const ctgb_plan* plan, const void* image, void* sino, int batch, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/* A^T: sinogram -> image. Replaces projection_t(): src/ctlib.cpp:71-84,
+ * prj_t_*_cuda (src/fan_ed_kernel.cu:1197-1229, src/fan_ea_kernel.cu:957-989,
+ * src/para_kernel.cu:716-745). */
+int ctgb_projection_t(const ctgb_plan* plan, const void* sino, void* image, int batch, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* B (weighted backprojector): sinogram -> image. Replaces backprojection():
+ * src/ctlib.cpp:30-43, bprj_*_cuda (src/fan_ed_kernel.cu:1265-1297,
+ * src/fan_ea_kernel.cu:1025-1057, src/para_kernel.cu:778-807). */
+int ctgb_backprojection(const ctgb_plan* plan, const void* sino, void* image, int batch, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* B^T: image -> sinogram. Replaces backprojection_t(): src/ctlib.cpp:15-28,
+ * bprj_t_*_cuda (src/fan_ed_kernel.cu:1231-1263, src/fan_ea_kernel.cu:991-1023,
+ * src/para_kernel.cu:747-776). */
+int ctgb_backprojection_t(const ctgb_plan* plan, const void* image, void* sino, int batch,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* RL-filtered backprojection: sinogram -> image. Replaces fbp():
+ * src/ctlib.cpp:86-99, fbp_*_cuda (src/fan_ed_kernel.cu:1333-1382,
+ * src/fan_ea_kernel.cu:1059-1107, src/para_kernel.cu:809-849). The ramp
+ * filter runs in fp32/fp64 FMA arithmetic (the reference's cuDNN convolution
+ * runs in TF32 unless the caller disables it). */
+int ctgb_fbp(const ctgb_plan* plan, const void* sino, void* image, int batch, void* workspace,
+             size_t workspace_bytes, void* stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* ctgb_last_error(void);
+
+/* ABI version, bumped on incompatible changes. */
+int ctgb_version(void);
+
+/* Host-side geometry of an options vector without touching a GPU (for tests
+ * and tooling). `what`: 0 flags (V ints as doubles: bit0 row lines, bit1
+ * flipped), 1 detector boundaries (V*(D+1)), 2 A/A^T factors (V*D),
+ * 3 line maps (V*L*4), 4 inverse seeds (V*5), 5 fbp pre-weight (D),
+ * 6 ramp taps (2D-1). Returns the element count, or -1 on error. */
+long ctgb_geometry_query(const double* options, int n_options, int dtype, int what, double* out,
+                         size_t n_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTGB_H */
