@@ -216,6 +216,15 @@ def run_ours(args):
     t_a = [ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)]
     t_at = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
     step_ms = sum(a + b for a, b in zip(t_a, t_at)) / args.steps
+    if args.only_step:
+        if rank == 0:
+            print(json.dumps({"only_step": True, "ms_per_step": step_ms, "ms_projection": statistics.mean(t_a),
+                              "ms_projection_t": statistics.mean(t_at),
+                              "value": ws * ru_step / (step_ms / 1e3), "unit": UNIT, "clocks": clocks}),
+                  flush=True)
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
     if ws > 1:
         t = torch.tensor([step_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -359,6 +368,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--only-step", action="store_true",
+                    help="time only the batched projection + projection_t step (for profiler runs)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1

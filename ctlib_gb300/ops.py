@@ -19,6 +19,7 @@ Differences from the reference, all on error paths or convenience:
 from __future__ import annotations
 
 import threading
+import weakref
 from collections import OrderedDict
 
 import torch
@@ -91,19 +92,25 @@ _FN = _FnTable()
 _plan_lock = threading.Lock()
 _plans: "OrderedDict[tuple, Plan]" = OrderedDict()
 _MAX_PLANS = 256
-_opt_cache: "OrderedDict[tuple, tuple]" = OrderedDict()
+# values of live CUDA options tensors: id -> (weakref, version, values). An
+# entry is used only while its weakref still points at the same object and the
+# version counter is unchanged (no in-place update); the finalizer drops it when
+# the tensor is collected, so a reused address or id never aliases.
+_opt_cache: dict = {}
 
 
 def _option_values(options) -> tuple:
     if isinstance(options, torch.Tensor):
-        key = (options.data_ptr(), options._version, str(options.device), options.numel(), options.dtype)
+        if not options.is_cuda:
+            return tuple(float(v) for v in options.detach().reshape(-1).tolist())
+        key = id(options)
         hit = _opt_cache.get(key)
-        if hit is not None:
-            return hit
+        if hit is not None and hit[0]() is options and hit[1] == options._version:
+            return hit[2]
         vals = tuple(float(v) for v in options.detach().reshape(-1).tolist())
-        _opt_cache[key] = vals
-        if len(_opt_cache) > 1024:
-            _opt_cache.popitem(last=False)
+        if hit is None or hit[0]() is not options:
+            weakref.finalize(options, _opt_cache.pop, key, None)
+        _opt_cache[key] = (weakref.ref(options), options._version, vals)
         return vals
     return tuple(float(v) for v in options)
 
