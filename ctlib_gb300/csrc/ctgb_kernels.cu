@@ -60,17 +60,28 @@ static int fail(int code, const std::string& msg) {
 // ----------------------------------------------------------------------------
 // device plan
 // ----------------------------------------------------------------------------
+// Coordinates are kept exact to ~1e-7 relative in fp32 by carrying every large
+// quantity as an unevaluated (hi, lo) pair built from the fp64 plan, and by
+// taking all differences that matter (cell boundary minus pixel edge) between
+// nearby numbers only: the detector gather anchors each cell boundary to the
+// integer pixel index it falls in and keeps the fraction, the image gather
+// anchors each pixel edge to the cell it falls in and keeps the offset. A and
+// A^T then evaluate the same overlaps to fp32 rounding, which keeps them
+// adjoint to ~1e-7 and within ~1e-7 of the fp64 evaluation.
 template <class T>
 struct DevPlan {
   int V, D, W, H, L, scan;
-  T dImg, s2r, x0, y0, dAng, wscale;
+  T dImg, s2r, dAng, wscale;
   const int* flags;   // V
-  const T* src;       // V*2
-  const T* db;        // V*(D+1)
-  const T* fq;        // V*D
-  const T* fbt;       // V*D
-  const T* lp;        // V*L*4
-  const float* inv;   // V*5
+  const T* src;       // V*2   source x, y
+  const T* db2;       // V*(D+1)*2  cell boundaries (hi, lo)
+  const T* wd;        // V*D   cell widths
+  const T* fq;        // V*D   A / A^T factor
+  const T* fbt;       // V*D   EA B^T factor
+  const T* lg;        // V*L*4 (1/sigma hi, 1/sigma lo, floor(beta), beta - floor(beta)), beta = -alpha/sigma
+  const T* ls;        // V*L   sigma
+  const T* lp;        // V*L*4 (alpha hi, alpha lo, sigma hi, sigma lo)
+  const float* inv;   // V*5   cell-index seed
   const T* rowc;      // H: row centre y
   const T* colc;      // W: column centre x
   const T* wpre;      // D
@@ -80,47 +91,66 @@ struct DevPlan {
 template <class T>
 struct VecT;
 template <>
-struct VecT<float> { using v4 = float4; using v2 = float2; };
+struct VecT<float> { using v2 = float2; };
 template <>
-struct VecT<double> { using v4 = double4; using v2 = double2; };
+struct VecT<double> { using v2 = double2; };
 
-template <class T, int SB>
-__device__ __forceinline__ void load_vec(const T* __restrict__ p, T (&v)[SB]) {
-  if constexpr (sizeof(T) == 4 && SB % 4 == 0) {
-#pragma unroll
-    for (int i = 0; i < SB / 4; ++i) {
-      float4 x = __ldg(reinterpret_cast<const float4*>(p) + i);
-      v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
-    }
-  } else if constexpr (SB % 2 == 0) {
-    using V2 = typename VecT<T>::v2;
-#pragma unroll
-    for (int i = 0; i < SB / 2; ++i) {
-      V2 x = __ldg(reinterpret_cast<const V2*>(p) + i);
-      v[2 * i] = x.x; v[2 * i + 1] = x.y;
-    }
+template <class T>
+struct Quad {
+  T x, y, z, w;
+};
+
+template <class T>
+__device__ __forceinline__ Quad<T> ld4(const T* p) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    return {a.x, a.y, a.z, a.w};
   } else {
-#pragma unroll
-    for (int i = 0; i < SB; ++i) v[i] = __ldg(p + i);
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return {a.x, a.y, b.x, b.y};
   }
 }
 
-template <class T, int SB>
-__device__ __forceinline__ void store_vec(T* p, const T (&v)[SB]) {
-  if constexpr (sizeof(T) == 4 && SB % 4 == 0) {
-#pragma unroll
-    for (int i = 0; i < SB / 4; ++i)
-      reinterpret_cast<float4*>(p)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-  } else if constexpr (SB % 2 == 0) {
+// SB slice values of one pixel / cell are stored as NQ planes of QW values;
+// consecutive pixels (cells) of one plane are contiguous, so the lanes of a
+// warp, which own consecutive cells (pixels), read contiguous vectors.
+template <int SB>
+struct Planes {
+  static constexpr int QW = SB >= 4 ? 4 : SB;
+  static constexpr int NQ = SB / QW;
+};
+
+template <class T, int QW>
+__device__ __forceinline__ void load_q(const T* __restrict__ p, T* v) {
+  if constexpr (sizeof(T) == 4 && QW == 4) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+  } else if constexpr (QW >= 2) {
     using V2 = typename VecT<T>::v2;
 #pragma unroll
-    for (int i = 0; i < SB / 2; ++i) {
+    for (int i = 0; i < QW / 2; ++i) {
+      const V2 x = __ldg(reinterpret_cast<const V2*>(p) + i);
+      v[2 * i] = x.x; v[2 * i + 1] = x.y;
+    }
+  } else {
+    v[0] = __ldg(p);
+  }
+}
+
+template <class T, int QW>
+__device__ __forceinline__ void store_q(T* p, const T* v) {
+  if constexpr (sizeof(T) == 4 && QW == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (QW >= 2) {
+    using V2 = typename VecT<T>::v2;
+#pragma unroll
+    for (int i = 0; i < QW / 2; ++i) {
       V2 x; x.x = v[2 * i]; x.y = v[2 * i + 1];
       reinterpret_cast<V2*>(p)[i] = x;
     }
   } else {
-#pragma unroll
-    for (int i = 0; i < SB; ++i) p[i] = v[i];
+    p[0] = v[0];
   }
 }
 
@@ -143,46 +173,50 @@ constexpr int kFoldEvery = 16;
 // ----------------------------------------------------------------------------
 // layout kernels
 // ----------------------------------------------------------------------------
-// image [B][H][W] -> rows [G][H][W][SB] and columns [G][W][H][SB] (k from the
-// bottom row), zero-padded to G*SB slices
+// image [B][H][W] -> row lines [G][H][NQ][W][QW] and column lines
+// [G][W][NQ][H][QW] (column walk index k = H-1-row), zero-padded to G*SB slices
 template <class T, int SB>
 __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T* __restrict__ imy, int B,
                                int H, int W, int G) {
-  const size_t n = (size_t)G * H * W;
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  const size_t n = (size_t)G * NQ * H * W;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % W);
     const int r = (int)((i / W) % H);
-    const int g = (int)(i / ((size_t)W * H));
-    T v[SB];
+    const int qd = (int)((i / ((size_t)W * H)) % NQ);
+    const int g = (int)(i / ((size_t)W * H * NQ));
+    T v[QW];
 #pragma unroll
-    for (int s = 0; s < SB; ++s) {
-      const int b = g * SB + s;
-      v[s] = b < B ? img[((size_t)b * H + r) * W + c] : T(0);
+    for (int j = 0; j < QW; ++j) {
+      const int b = g * SB + qd * QW + j;
+      v[j] = b < B ? img[((size_t)b * H + r) * W + c] : T(0);
     }
-    store_vec<T, SB>(imx + i * SB, v);
-    if (imy) store_vec<T, SB>(imy + (((size_t)g * W + c) * H + (H - 1 - r)) * SB, v);
+    store_q<T, QW>(imx + ((((size_t)g * H + r) * NQ + qd) * W + c) * QW, v);
+    store_q<T, QW>(imy + ((((size_t)g * W + c) * NQ + qd) * H + (H - 1 - r)) * QW, v);
   }
 }
 
-// sinogram [B][V][D] (external detector order) -> [G][V][D][SB] (internal,
-// increasing-boundary order), times an optional per-(view, cell) factor
+// sinogram [B][V][D] (external detector order) -> [G][V][NQ][D][QW]
+// (increasing-boundary order), times an optional per-(view, cell) factor
 template <class T, int SB>
 __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const int* __restrict__ flags,
                               const T* __restrict__ f, int B, int V, int D, int G) {
-  const size_t n = (size_t)G * V * D;
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  const size_t n = (size_t)G * V * NQ * D;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int d = (int)(i % D);
-    const int v = (int)((i / D) % V);
-    const int g = (int)(i / ((size_t)D * V));
+    const int qd = (int)((i / D) % NQ);
+    const int v = (int)((i / ((size_t)D * NQ)) % V);
+    const int g = (int)(i / ((size_t)D * NQ * V));
     const int de = (flags[v] & 2) ? D - 1 - d : d;
     const T fac = f ? f[(size_t)v * D + d] : T(1);
-    T val[SB];
+    T val[QW];
 #pragma unroll
-    for (int s = 0; s < SB; ++s) {
-      const int b = g * SB + s;
-      val[s] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
+    for (int j = 0; j < QW; ++j) {
+      const int b = g * SB + qd * QW + j;
+      val[j] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
     }
-    store_vec<T, SB>(q + i * SB, val);
+    store_q<T, QW>(q + i * QW, val);
   }
 }
 
@@ -204,9 +238,14 @@ __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
 // ----------------------------------------------------------------------------
 // detector gather: A (kind kA) and B^T (kind kBt)
 // ----------------------------------------------------------------------------
+// Thread = (view v, cell d), SB slices. Per line: the cell's lower boundary in
+// pixel-edge units is u = db*(1/sigma) + beta; it is split into an integer
+// anchor k and a fraction f computed from exact products (two-product via FMA),
+// and the cell spans [f, f + w/sigma) pixels from k on.
 template <class T, int SB, int KIND>
 __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
                                                     const T* __restrict__ imy, T* __restrict__ out, int B) {
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
   const int v = blockIdx.y * 8 + warp;
@@ -214,145 +253,197 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
   if (v >= P.V || d >= P.D) return;
   const int fl = P.flags[v];
   const bool xb = fl & 1;
-  const T* dbv = P.db + (size_t)v * (P.D + 1);
-  const T dlo = dbv[d], dhi = dbv[d + 1];
   const int nlines = xb ? P.H : P.W;
   const int N = xb ? P.W : P.H;
-  const T* base = xb ? imx + (size_t)g * P.H * P.W * SB : imy + (size_t)g * P.W * P.H * SB;
-  const T* lpv = P.lp + (size_t)v * P.L * 4;
+  const T* base = (xb ? imx : imy) + (size_t)g * P.H * P.W * SB;
+  const size_t bi = ((size_t)v * (P.D + 1) + d) * 2;
+  const T Dh = P.db2[bi], Dl = P.db2[bi + 1];
+  const T wcell = P.wd[(size_t)v * P.D + d];
+  const T* lgv = P.lg + (size_t)v * P.L * 4;
+  const T* lsv = P.ls + (size_t)v * P.L;
   T sx = T(0), sy = T(0);
   if (KIND == kBt && P.scan != kPara) { sx = P.src[2 * v]; sy = P.src[2 * v + 1]; }
+  const T pc0 = xb ? P.colc[0] : P.rowc[P.H - 1];  // centre of pixel k = 0 along the walk
 
   T sum[SB], comp[SB], blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) { sum[s] = T(0); comp[s] = T(0); blk[s] = T(0); }
 
   for (int l = 0; l < nlines; ++l) {
-    const T sigma = lpv[4 * l + 1], beta = lpv[4 * l + 2], gam = lpv[4 * l + 3];
-    const T tlo = fma(dlo, gam, beta), thi = fma(dhi, gam, beta);
-    const T a = tlo > T(0) ? tlo : T(0);
-    const T b = thi < T(N) ? thi : T(N);
-    if (a < b) {
-      const int k0 = (int)floor(a);
-      int k1 = (int)ceil(b);
-      if (k1 > N) k1 = N;
-      const T* row = base + (size_t)l * N * SB;
-      T lc = T(0);
-      if (KIND == kBt && P.scan != kPara) lc = xb ? P.rowc[l] : P.colc[l];
-      for (int k = k0; k < k1; ++k) {
-        const T lo = a > T(k) ? a : T(k);
-        const T hi = b < T(k + 1) ? b : T(k + 1);
-        T w = hi - lo;
+    const auto G4 = ld4<T>(lgv + 4 * l);
+    const T ph = Dh * G4.x;
+    const T pl = fma(Dh, G4.x, -ph);
+    const T corr = fma(Dl, G4.x, fma(Dh, G4.y, pl)) + G4.w;
+    const T kaf = floor((ph + G4.z) + corr);
+    T f = (ph - (kaf - G4.z)) + corr;
+    int k = (int)kaf;
+    if (f < T(0)) { f += T(1); --k; }
+    T a = f;
+    T b = fma(wcell, G4.x, f);
+    if (k < 0) {  // cell starts left of the image: move to pixel 0
+      const T sh = T(-k);
+      a -= sh;
+      b -= sh;
+      k = 0;
+    }
+    if (k >= N || b <= T(0)) {
+      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
+      continue;
+    }
+    const T sig = lsv[l];
+    const T* row = base + (size_t)l * N * SB;
+    T lc = T(0);
+    if (KIND == kBt && P.scan != kPara) lc = xb ? P.rowc[l] : P.colc[l];
+    while (true) {
+      const T ov = (b < T(1) ? b : T(1)) - (a > T(0) ? a : T(0));
+      if (ov > T(0)) {
+        T w = ov;
         if (KIND == kA) {
-          w *= sigma;
+          w *= sig;
         } else if (P.scan == kFanED) {
-          const T pc = fma(T(k) + T(0.5), P.dImg, xb ? P.x0 : P.y0);
+          const T pc = fma(T(k), P.dImg, pc0);
           w *= xb ? cweight_ed(sx, sy, pc, lc, P.s2r) : cweight_ed(sx, sy, lc, pc, P.s2r);
         } else if (P.scan == kFanEA) {
-          const T pc = fma(T(k) + T(0.5), P.dImg, xb ? P.x0 : P.y0);
+          const T pc = fma(T(k), P.dImg, pc0);
           w /= xb ? dist2_ea(sx, sy, pc, lc) : dist2_ea(sx, sy, lc, pc);
         }
-        T u[SB];
-        load_vec<T, SB>(row + (size_t)k * SB, u);
+        const T* px = row + (size_t)k * QW;
 #pragma unroll
-        for (int s = 0; s < SB; ++s) blk[s] = fma(w, u[s], blk[s]);
+        for (int qd = 0; qd < NQ; ++qd) {
+          T u[QW];
+          load_q<T, QW>(px + (size_t)qd * N * QW, u);
+#pragma unroll
+          for (int j = 0; j < QW; ++j) blk[qd * QW + j] = fma(w, u[j], blk[qd * QW + j]);
+        }
       }
+      b -= T(1);
+      if (b <= T(0) || ++k >= N) break;
+      a -= T(1);
     }
     if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
   }
   kahan_fold<T, SB>(sum, comp, blk);
-  T f = T(1);
-  if (KIND == kA) f = P.fq[(size_t)v * P.D + d];
-  else if (P.scan == kFanEA) f = P.fbt[(size_t)v * P.D + d];
+  T fac = T(1);
+  if (KIND == kA) fac = P.fq[(size_t)v * P.D + d];
+  else if (P.scan == kFanEA) fac = P.fbt[(size_t)v * P.D + d];
   const int de = (fl & 2) ? P.D - 1 - d : d;
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
-    if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = sum[s] * f;
+    if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = sum[s] * fac;
   }
 }
 
 // ----------------------------------------------------------------------------
 // image gather: A^T (kind kAt) and B (kind kB)
 // ----------------------------------------------------------------------------
+// Thread = pixel (r, c), SB slices, loop over views. Per view the pixel's lower
+// edge x = alpha + sigma*k is formed as an unevaluated pair (two-product and
+// two-sum), its cell d is seeded from the closed-form inverse of the boundary
+// map and corrected against the stored boundaries, and the offset a = x - db[d]
+// is taken between the two nearby pairs; the cells then follow by widths.
+constexpr int kViewChunk = 128;
+
 template <class T, int SB, int KIND>
 __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __restrict__ q, T* __restrict__ img,
                                                     int B, T out_mul, T out_div) {
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  __shared__ float s_inv[kViewChunk][5];
+  __shared__ int s_flag[kViewChunk];
+  __shared__ T s_src[kViewChunk][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
   const int r = blockIdx.y * 8 + warp;
   const int g = blockIdx.z;
-  if (c >= P.W || r >= P.H) return;
-  const T* qg = q + (size_t)g * P.V * P.D * SB;
-  // pixel centre (for the backprojector weights)
-  const T pcx = fma(T(c) + T(0.5), P.dImg, P.x0);
-  const T pcy = P.rowc[r];
+  const bool active = c < P.W && r < P.H;
+  const int D = P.D;
+  const T* qg = q + (size_t)g * P.V * D * SB;
+  const T pcx = active ? P.colc[c] : T(0);
+  const T pcy = active ? P.rowc[r] : T(0);
+  const bool ea = P.scan == kFanEA;
 
   T sum[SB], comp[SB], blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) { sum[s] = T(0); comp[s] = T(0); blk[s] = T(0); }
 
-  for (int v = 0; v < P.V; ++v) {
-    const int fl = P.flags[v];
-    const bool xb = fl & 1;
-    const int line = xb ? r : c;
-    const int k = xb ? c : P.H - 1 - r;
-    const T* lpl = P.lp + ((size_t)v * P.L + line) * 4;
-    const T alpha = lpl[0], sigma = lpl[1];
-    const T xlo = fma(sigma, T(k), alpha);
-    const T xhi = fma(sigma, T(k + 1), alpha);
-    // seed the cell index from the closed-form inverse of the boundary map
-    const float* iv = P.inv + (size_t)v * 5;
-    const float xf = (float)xlo;
-    float u = xf * iv[0] / fmaf(xf, iv[2], iv[1]);
-    if (P.scan == kFanEA) u = atanf(u);
-    const float cb = fmaf(iv[4], u, iv[3]);
-    const int D = P.D;
-    int d = cb < 0.f ? 0 : (cb >= (float)(D - 1) ? D - 1 : (int)cb);
-    const T* dbv = P.db + (size_t)v * (D + 1);
-    while (d > 0 && xlo < dbv[d]) --d;
-    while (d < D - 1 && dbv[d + 1] <= xlo) ++d;
-    T vacc[SB];
-    if (KIND == kB) {
+  for (int v0 = 0; v0 < P.V; v0 += kViewChunk) {
+    const int nv = min(kViewChunk, P.V - v0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+      s_flag[i] = P.flags[v0 + i];
 #pragma unroll
-      for (int s = 0; s < SB; ++s) vacc[s] = T(0);
+      for (int j = 0; j < 5; ++j) s_inv[i][j] = P.inv[(size_t)(v0 + i) * 5 + j];
+      s_src[i][0] = P.src[2 * (v0 + i)];
+      s_src[i][1] = P.src[2 * (v0 + i) + 1];
     }
-    T lob = dbv[d];
-    const T* qv = qg + (size_t)v * D * SB;
-    for (; d < D; ++d) {
-      const T hib = dbv[d + 1];
-      const T lo = xlo > lob ? xlo : lob;
-      const T hi = xhi < hib ? xhi : hib;
-      if (lo >= xhi) break;
-      if (hi > lo) {
-        const T w = hi - lo;
-        T qq[SB];
-        load_vec<T, SB>(qv + (size_t)d * SB, qq);
-        if (KIND == kAt) {
+    __syncthreads();
+    if (!active) continue;
+    for (int j = 0; j < nv; ++j) {
+      const int v = v0 + j;
+      const bool xb = s_flag[j] & 1;
+      const int line = xb ? r : c;
+      const int k = xb ? c : P.H - 1 - r;
+      const auto A4 = ld4<T>(P.lp + ((size_t)v * P.L + line) * 4);
+      const T kf = T(k);
+      // x = alpha + sigma*k as (xs, xl)
+      const T qh = A4.z * kf;
+      const T ql = fma(A4.z, kf, -qh);
+      const T xs = A4.x + qh;
+      const T bv = xs - A4.x;
+      const T xe = (A4.x - (xs - bv)) + (qh - bv);
+      const T xl = xe + (A4.y + fma(A4.w, kf, ql));
+      // seed the cell
+      const float xf = (float)xs;
+      float u = __fdividef(xf * s_inv[j][0], fmaf(xf, s_inv[j][2], s_inv[j][1]));
+      if (ea) u = atanf(u);
+      const float cb = fmaf(s_inv[j][4], u, s_inv[j][3]);
+      int d = cb < 0.f ? 0 : (cb >= (float)(D - 1) ? D - 1 : (int)cb);
+      const T* db2v = P.db2 + (size_t)v * (D + 1) * 2;
+      while (d > 0 && xs < db2v[2 * d]) --d;
+      while (d < D - 1 && db2v[2 * d + 2] <= xs) ++d;
+      const T* wdv = P.wd + (size_t)v * D;
+      T a = (xs - db2v[2 * d]) + (xl - db2v[2 * d + 1]);
+      if (a < T(0) && d > 0) { --d; a += wdv[d]; }
+      T b = a + (A4.z + A4.w);
+      T vacc[SB];
+      if (KIND == kB) {
 #pragma unroll
-          for (int s = 0; s < SB; ++s) blk[s] = fma(w, qq[s], blk[s]);
-        } else {
+        for (int s = 0; s < SB; ++s) vacc[s] = T(0);
+      }
+      const T* qv = qg + (size_t)v * D * SB;
+      while (d < D) {
+        const T w = wdv[d];
+        const T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+        if (ov > T(0)) {
 #pragma unroll
-          for (int s = 0; s < SB; ++s) vacc[s] = fma(w, qq[s], vacc[s]);
+          for (int qd = 0; qd < NQ; ++qd) {
+            T qq[QW];
+            load_q<T, QW>(qv + ((size_t)qd * D + d) * QW, qq);
+#pragma unroll
+            for (int i = 0; i < QW; ++i) {
+              if (KIND == kAt) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
+              else vacc[qd * QW + i] = fma(ov, qq[i], vacc[qd * QW + i]);
+            }
+          }
         }
+        b -= w;
+        if (b <= T(0)) break;
+        a -= w;
+        ++d;
       }
-      if (hib >= xhi) break;
-      lob = hib;
-    }
-    if (KIND == kB) {
-      T wv;
-      if (P.scan == kFanED) {
-        wv = cweight_ed(P.src[2 * v], P.src[2 * v + 1], pcx, pcy, P.s2r) / sigma;
-      } else if (P.scan == kFanEA) {
-        wv = T(1) / (dist2_ea(P.src[2 * v], P.src[2 * v + 1], pcx, pcy) * sigma);
-      } else {
-        wv = T(1) / P.dImg;
-      }
+      if (KIND == kB) {
+        const T sig = A4.z + A4.w;
+        T wv;
+        if (P.scan == kFanED) wv = cweight_ed(s_src[j][0], s_src[j][1], pcx, pcy, P.s2r) / sig;
+        else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(s_src[j][0], s_src[j][1], pcx, pcy) * sig);
+        else wv = T(1) / P.dImg;
 #pragma unroll
-      for (int s = 0; s < SB; ++s) blk[s] = fma(vacc[s], wv, blk[s]);
+        for (int s = 0; s < SB; ++s) blk[s] = fma(vacc[s], wv, blk[s]);
+      }
+      if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
     }
-    if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
   }
+  if (!active) return;
   kahan_fold<T, SB>(sum, comp, blk);
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
@@ -420,7 +511,7 @@ __global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __re
       if (k < D) {
         const T val = fma(h0, row[k], acc[i]);
         const int di = flip ? D - 1 - k : k;
-        qv[(size_t)di * SB + s] = val;
+        qv[((size_t)(s / Planes<SB>::QW) * D + di) * Planes<SB>::QW + (s % Planes<SB>::QW)] = val;
       }
     }
   }
@@ -446,16 +537,32 @@ template <class T>
 static int upload(ctgb_plan* p) {
   const HostGeom& g = p->geom;
   const int V = g.V, D = g.D, L = g.L;
-  // table sizes in elements of T
-  std::vector<std::pair<const std::vector<double>*, size_t>> parts;
-  std::vector<double> rowc(g.H), colc(g.W);
-  for (int r = 0; r < g.H; ++r) rowc[r] = (double)(T)(((double)((T)(g.height / 2) - (T)r) - 0.5) * g.dImg);
-  for (int c = 0; c < g.W; ++c) colc[c] = (double)(T)(((double)((T)c - (T)(g.width / 2)) + 0.5) * g.dImg);
-  const std::vector<const std::vector<double>*> tabs = {&g.src, &g.db, &g.fq, &g.fbt, &g.lp,
+  auto split_hi = [](double x) { return (double)(T)x; };
+  // tables in elements of T, each built in double and rounded once
+  std::vector<double> db2((size_t)V * (D + 1) * 2), lg((size_t)V * L * 4, 0.0), ls((size_t)V * L, 1.0),
+      lp((size_t)V * L * 4, 0.0), rowc(g.H), colc(g.W);
+  for (size_t i = 0; i < g.db.size(); ++i) {
+    const double hi = split_hi(g.db[i]);
+    db2[2 * i] = hi;
+    db2[2 * i + 1] = g.db[i] - hi;
+  }
+  for (size_t i = 0; i < (size_t)V * L; ++i) {
+    const double alpha = g.lp[2 * i], sigma = g.lp[2 * i + 1];
+    if (!(sigma > 0)) continue;  // unused line slot (lines = min(H, W) for this view)
+    const double gam = 1.0 / sigma, beta = -alpha / sigma;
+    const double gh = split_hi(gam), bi = std::floor(beta);
+    lg[4 * i] = gh; lg[4 * i + 1] = gam - gh; lg[4 * i + 2] = bi; lg[4 * i + 3] = beta - bi;
+    ls[i] = sigma;
+    const double ah = split_hi(alpha), sh = split_hi(sigma);
+    lp[4 * i] = ah; lp[4 * i + 1] = alpha - ah; lp[4 * i + 2] = sh; lp[4 * i + 3] = sigma - sh;
+  }
+  for (int r = 0; r < g.H; ++r) rowc[r] = (g.height / 2 - r - 0.5) * g.dImg;
+  for (int c = 0; c < g.W; ++c) colc[c] = (c - g.width / 2 + 0.5) * g.dImg;
+  const std::vector<const std::vector<double>*> tabs = {&g.src, &db2, &g.wd, &g.fq, &g.fbt, &lg, &ls, &lp,
                                                         &rowc, &colc, &g.wpre, &g.taps};
   size_t off = 0;
   std::vector<size_t> offs;
-  auto align = [](size_t x) { return (x + 31) & ~(size_t)31; };
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
   for (auto* t : tabs) { offs.push_back(off); off = align(off + t->size() * sizeof(T)); }
   const size_t off_flags = off; off = align(off + (size_t)V * sizeof(int));
   const size_t off_inv = off; off = align(off + (size_t)V * 5 * sizeof(float));
@@ -473,17 +580,19 @@ static int upload(ctgb_plan* p) {
   unsigned char* b = static_cast<unsigned char*>(p->dev);
   DevPlan<T> P{};
   P.V = V; P.D = D; P.W = g.W; P.H = g.H; P.L = L; P.scan = g.scan;
-  P.dImg = (T)g.dImg; P.s2r = (T)g.s2r; P.x0 = (T)g.x0; P.y0 = (T)g.y0; P.dAng = (T)g.dAng;
-  P.wscale = (T)g.wscale;
+  P.dImg = (T)g.dImg; P.s2r = (T)g.s2r; P.dAng = (T)g.dAng; P.wscale = (T)g.wscale;
   P.src = reinterpret_cast<const T*>(b + offs[0]);
-  P.db = reinterpret_cast<const T*>(b + offs[1]);
-  P.fq = reinterpret_cast<const T*>(b + offs[2]);
-  P.fbt = reinterpret_cast<const T*>(b + offs[3]);
-  P.lp = reinterpret_cast<const T*>(b + offs[4]);
-  P.rowc = reinterpret_cast<const T*>(b + offs[5]);
-  P.colc = reinterpret_cast<const T*>(b + offs[6]);
-  P.wpre = reinterpret_cast<const T*>(b + offs[7]);
-  P.taps = reinterpret_cast<const T*>(b + offs[8]);
+  P.db2 = reinterpret_cast<const T*>(b + offs[1]);
+  P.wd = reinterpret_cast<const T*>(b + offs[2]);
+  P.fq = reinterpret_cast<const T*>(b + offs[3]);
+  P.fbt = reinterpret_cast<const T*>(b + offs[4]);
+  P.lg = reinterpret_cast<const T*>(b + offs[5]);
+  P.ls = reinterpret_cast<const T*>(b + offs[6]);
+  P.lp = reinterpret_cast<const T*>(b + offs[7]);
+  P.rowc = reinterpret_cast<const T*>(b + offs[8]);
+  P.colc = reinterpret_cast<const T*>(b + offs[9]);
+  P.wpre = reinterpret_cast<const T*>(b + offs[10]);
+  P.taps = reinterpret_cast<const T*>(b + offs[11]);
   P.flags = reinterpret_cast<const int*>(b + off_flags);
   P.inv = reinterpret_cast<const float*>(b + off_inv);
   if constexpr (sizeof(T) == 4) p->pf = P; else p->pd = P;

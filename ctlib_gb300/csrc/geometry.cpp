@@ -1,6 +1,9 @@
-// Host-side scan geometry (see geometry.h). Expressions that the reference
-// evaluates in scalar_t are evaluated in T here, those it evaluates in double
-// are evaluated in double, so the rounded boundaries match the reference's.
+// Host-side scan geometry (see geometry.h). The view angle is formed in the
+// data type exactly as the reference forms it (src/fan_ed_kernel.cu:61), so the
+// branch and flip decisions are the reference's; everything continuous after
+// that (source position, boundaries, widths, line maps, normalisation) is
+// evaluated in fp64, which makes the tables the FP64 evaluation of the
+// reference's formulas. The kernels consume them as (hi, lo) pairs.
 #include "geometry.h"
 
 #include <cmath>
@@ -44,22 +47,23 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
   g.flags.assign(V, 0);
   g.src.assign((size_t)V * 2, 0.0);
   g.db.assign((size_t)V * (D + 1), 0.0);
+  g.wd.assign((size_t)V * D, 0.0);
   g.fq.assign((size_t)V * D, 0.0);
   g.fbt.assign((size_t)V * D, 1.0);
-  g.lp.assign((size_t)V * L * 4, 0.0);
+  g.lp.assign((size_t)V * L * 2, 0.0);
   g.inv.assign((size_t)V * 5, 0.0);
 
   const double PI = std::acos(-1.0);
-  const T x0 = -width / 2 * dImg;   // src/fan_ed_kernel.cu:107
-  const T y0 = -height / 2 * dImg;  // src/fan_ed_kernel.cu:196
+  const double x0 = -(double)width / 2 * (double)dImg;   // left image edge (src/fan_ed_kernel.cu:107)
+  const double y0 = -(double)height / 2 * (double)dImg;  // bottom image edge (src/fan_ed_kernel.cu:196)
   g.x0 = x0; g.y0 = y0;
-  // virtual detector pitch/shift: scalar_t expressions widened to double (:68-69)
-  const double virdDet = (double)(s2r / (s2r + d2r) * dDet);
-  const double virshift = (double)(s2r / (s2r + d2r) * binshift);
+  // virtual detector pitch / shift (src/fan_ed_kernel.cu:68-69)
+  const double virdDet = (double)s2r / ((double)s2r + (double)d2r) * (double)dDet;
+  const double virshift = (double)s2r / ((double)s2r + (double)d2r) * (double)binshift;
   const double R = (double)s2r;
-  double max_half_x = std::fabs((double)x0), max_half_y = std::fabs((double)y0);
+  double max_half_x = std::fabs(x0), max_half_y = std::fabs(y0);
 
-  std::vector<T> dbT(D + 1), cosb(D + 1);
+  std::vector<double> cosb(D + 1);
   for (int v = 0; v < V; ++v) {
     const double ang = (double)((T)v * dAng + Ang0);  // src/fan_ed_kernel.cu:61
     const bool xb = std::fabs(ang - std::round(ang / PI) * PI) * 4 / PI <= 1;
@@ -67,84 +71,81 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
     const bool flip = e2 >= 3 && e2 < 7;
     const double c = std::cos(ang), s = std::sin(ang);
     g.flags[v] = (xb ? 1 : 0) | (flip ? 2 : 0);
-    const T sx = (T)(-s * (double)s2r), sy = (T)(c * (double)s2r);
+    const double sx = -s * (double)s2r, sy = c * (double)s2r;
     g.src[2 * v] = sx; g.src[2 * v + 1] = sy;
     if (g.scan != kPara) {
       // the source must stay outside the image along the integration lines
-      if ((xb && std::fabs((double)sy) <= max_half_y) || (!xb && std::fabs((double)sx) <= max_half_x)) {
+      if ((xb && std::fabs(sy) <= max_half_y) || (!xb && std::fabs(sx) <= max_half_x)) {
         err = "source lies inside the image field of view";
         return false;
       }
     }
     const double e = flip ? -1.0 : 1.0;
+    double* dbv = &g.db[(size_t)v * (D + 1)];
     for (int b = 0; b <= D; ++b) {
-      const T tb = flip ? (dets / 2 - (T)b) : ((T)b - dets / 2);
-      T val;
+      const double tb = flip ? ((double)dets / 2 - b) : (b - (double)dets / 2);
+      double val;
       if (g.scan == kFanED) {
-        const double sdet = (double)tb * virdDet + virshift;
-        const T detx = (T)(sdet * c), dety = (T)(sdet * s);
+        const double sdet = tb * virdDet + virshift;
+        const double detx = sdet * c, dety = sdet * s;
         val = xb ? map_x(sx, sy, detx, dety) : map_y(sx, sy, detx, dety);
       } else if (g.scan == kFanEA) {
-        const double beta = (double)(tb * dDet + binshift) + ang;
-        val = xb ? (T)((double)sx + std::sin(beta) / std::cos(beta) * (double)sy)
-                 : (T)((double)sy + std::cos(beta) / std::sin(beta) * (double)sx);
+        const double beta = tb * (double)dDet + (double)binshift + ang;
+        val = xb ? sx + std::sin(beta) / std::cos(beta) * sy : sy + std::cos(beta) / std::sin(beta) * sx;
       } else {
-        const T num = tb * dDet + binshift;
-        val = (T)((double)num / (xb ? c : s));
+        val = (tb * (double)dDet + (double)binshift) / (xb ? c : s);
       }
-      dbT[b] = val;
-      g.db[(size_t)v * (D + 1) + b] = (double)val;
+      dbv[b] = val;
     }
     for (int b = 0; b < D; ++b) {
-      if (!(dbT[b + 1] > dbT[b])) {
+      if (!(dbv[b + 1] > dbv[b])) {
         err = "detector boundaries are not strictly increasing on the projection axis";
         return false;
       }
+      g.wd[(size_t)v * D + b] = dbv[b + 1] - dbv[b];
     }
     if (g.scan != kPara) {
       for (int b = 0; b <= D; ++b) {
-        const T u = dbT[b];
+        const double u = dbv[b];
         cosb[b] = xb ? std::fabs(sy) / std::sqrt((u - sx) * (u - sx) + sy * sy)
                      : std::fabs(sx) / std::sqrt((u - sy) * (u - sy) + sx * sx);
       }
       for (int d = 0; d < D; ++d) {
-        const T cbar = (cosb[d + 1] + cosb[d]) / 2;
-        const T w = dbT[d + 1] - dbT[d];
-        g.fq[(size_t)v * D + d] = (double)dImg / ((double)cbar * (double)w);
-        if (g.scan == kFanEA) g.fbt[(size_t)v * D + d] = (double)dImg / (double)cbar;
+        const double cbar = (cosb[d + 1] + cosb[d]) / 2;
+        g.fq[(size_t)v * D + d] = (double)dImg / (cbar * g.wd[(size_t)v * D + d]);
+        if (g.scan == kFanEA) g.fbt[(size_t)v * D + d] = (double)dImg / cbar;
       }
     } else {
-      const T dinterval = dImg / dDet;
-      for (int d = 0; d < D; ++d) g.fq[(size_t)v * D + d] = (double)dinterval;
+      for (int d = 0; d < D; ++d) g.fq[(size_t)v * D + d] = (double)dImg / (double)dDet;
     }
     // per-line affine pixel-edge maps
     const int nl = xb ? g.H : g.W;
     for (int l = 0; l < nl; ++l) {
       double alpha, sigma;
       if (xb) {
-        const T i0y = (T)(((double)(height / 2 - (T)l) - 0.5) * (double)dImg);
+        const double i0y = ((double)height / 2 - l - 0.5) * (double)dImg;
         if (g.scan != kPara) {
-          const double den = (double)i0y - (double)sy;
-          alpha = ((double)sx * (double)i0y - (double)sy * (double)x0) / den;
-          sigma = -(double)sy * (double)dImg / den;
+          const double den = i0y - sy;
+          alpha = (sx * i0y - sy * (double)x0) / den;
+          sigma = -sy * (double)dImg / den;
         } else {
-          alpha = s / c * (double)i0y + (double)x0;
+          alpha = s / c * i0y + (double)x0;
           sigma = (double)dImg;
         }
       } else {
-        const T i0x = (T)(((double)((T)l - width / 2) + 0.5) * (double)dImg);
+        const double i0x = (l - (double)width / 2 + 0.5) * (double)dImg;
         if (g.scan != kPara) {
-          const double den = (double)i0x - (double)sx;
-          alpha = ((double)sy * (double)i0x - (double)sx * (double)y0) / den;
-          sigma = -(double)sx * (double)dImg / den;
+          const double den = i0x - sx;
+          alpha = (sy * i0x - sx * (double)y0) / den;
+          sigma = -sx * (double)dImg / den;
         } else {
-          alpha = (double)y0 + c / s * (double)i0x;
+          alpha = (double)y0 + c / s * i0x;
           sigma = (double)dImg;
         }
       }
       if (!(sigma > 0)) { err = "degenerate pixel projection (source inside the image?)"; return false; }
-      double* q = &g.lp[((size_t)v * L + l) * 4];
-      q[0] = alpha; q[1] = sigma; q[2] = -alpha / sigma; q[3] = 1.0 / sigma;
+      double* q = &g.lp[((size_t)v * L + l) * 2];
+      q[0] = alpha; q[1] = sigma;
     }
     // inverse boundary map seed
     double* P = &g.inv[(size_t)v * 5];

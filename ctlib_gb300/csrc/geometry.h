@@ -5,9 +5,10 @@
 //     columns otherwise) and the detector-order flip, decided exactly as the
 //     reference does (src/fan_ed_kernel.cu:61-77);
 //   * the D+1 detector-cell boundaries projected onto the view's axis
-//     (x-axis for row lines, y-axis for column lines), rounded to the data type
-//     at the same points as the reference (src/fan_ed_kernel.cu:78-95,
-//     src/fan_ea_kernel.cu:72-84, src/para_kernel.cu:52-60), in increasing order;
+//     (x-axis for row lines, y-axis for column lines), evaluated in fp64 with
+//     the reference's formulas (src/fan_ed_kernel.cu:78-95,
+//     src/fan_ea_kernel.cu:72-84, src/para_kernel.cu:52-60), in increasing
+//     order, plus the cell widths (fp64 differences);
 //   * per-detector normalisation factors;
 //   * an approximate inverse of the boundary map (axis coordinate -> fractional
 //     cell index) used to seed the cell search in the image-side gather;
@@ -31,9 +32,10 @@ struct HostGeom {
   std::vector<int32_t> flags;  // V: bit0 row lines (x-branch), bit1 flipped detector order
   std::vector<double> src;     // V*2: source x, y (fan)
   std::vector<double> db;      // V*(D+1): cell boundaries on the axis, increasing
+  std::vector<double> wd;      // V*D: cell widths db[d+1]-db[d]
   std::vector<double> fq;      // V*D: A / A^T factor (fan dImg/(cbar*w), para dImg/dDet)
   std::vector<double> fbt;     // V*D: extra B^T factor (EA: dImg/cbar), 1 otherwise
-  std::vector<double> lp;      // V*L*4: alpha, sigma, -alpha/sigma, 1/sigma
+  std::vector<double> lp;      // V*L*2: alpha, sigma (pixel edge k of a line maps to alpha + sigma*k)
   std::vector<double> inv;     // V*5: guess u = x*P0/(P1+x*P2) (atan for EA), cell = P3+P4*u
   std::vector<double> wpre;    // D: fbp detector pre-weight, applied as (y * wpre[k]) * wscale
   double wscale = 1.0;

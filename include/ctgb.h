@@ -103,7 +103,7 @@ int ctgb_version(void);
 /* Host-side geometry of an options vector without touching a GPU (for tests
  * and tooling). `what`: 0 flags (V ints as doubles: bit0 row lines, bit1
  * flipped), 1 detector boundaries (V*(D+1)), 2 A/A^T factors (V*D),
- * 3 line maps (V*L*4), 4 inverse seeds (V*5), 5 fbp pre-weight (D),
+ * 3 line maps (V*L*2: alpha, sigma), 4 inverse seeds (V*5), 5 fbp pre-weight (D),
  * 6 ramp taps (2D-1). Returns the element count, or -1 on error. */
 long ctgb_geometry_query(const double* options, int n_options, int dtype, int what, double* out,
                          size_t n_out);

@@ -86,7 +86,7 @@ def test_line_maps_reproduce_pixel_edges(native, opts):
     (map_x / map_y, src/fan_ed_kernel.cu:8-15) or along the rays (parallel)."""
     V, D, W, H = (int(opts[i]) for i in range(4))
     L = max(W, H)
-    lp = _query(native, opts, 3, dtype=1).reshape(V, L, 4)
+    lp = _query(native, opts, 3, dtype=1).reshape(V, L, 2)
     flags = _query(native, opts, 0).astype(int)
     dImg = opts[4]
     scan = int(opts[-1])
