@@ -154,14 +154,24 @@ __device__ __forceinline__ void store_q(T* p, const T* v) {
   }
 }
 
+// Round-to-nearest multiply / add that the compiler never contracts into an
+// FMA: the two-product and two-sum steps below are exact only if the product
+// and the sums they correct are the rounded ones.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
 // Kahan fold of a block partial into (sum, comp); the partial is reset.
 template <class T, int SB>
 __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)[SB]) {
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
-    T y = blk[s] - comp[s];
-    T t = sum[s] + y;
-    comp[s] = (t - sum[s]) - y;
+    const T y = sub_rn(blk[s], comp[s]);
+    const T t = add_rn(sum[s], y);
+    comp[s] = sub_rn(sub_rn(t, sum[s]), y);
     sum[s] = t;
     blk[s] = T(0);
   }
@@ -169,6 +179,8 @@ __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)
 
 enum Kind { kA = 0, kBt = 1, kAt = 2, kB = 3 };
 constexpr int kFoldEvery = 16;
+
+
 
 // ----------------------------------------------------------------------------
 // layout kernels
@@ -271,11 +283,11 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
 
   for (int l = 0; l < nlines; ++l) {
     const auto G4 = ld4<T>(lgv + 4 * l);
-    const T ph = Dh * G4.x;
+    const T ph = mul_rn(Dh, G4.x);
     const T pl = fma(Dh, G4.x, -ph);
-    const T corr = fma(Dl, G4.x, fma(Dh, G4.y, pl)) + G4.w;
-    const T kaf = floor((ph + G4.z) + corr);
-    T f = (ph - (kaf - G4.z)) + corr;
+    const T corr = add_rn(fma(Dl, G4.x, fma(Dh, G4.y, pl)), G4.w);
+    const T kaf = floor(add_rn(add_rn(ph, G4.z), corr));
+    T f = add_rn(sub_rn(ph, sub_rn(kaf, G4.z)), corr);
     int k = (int)kaf;
     if (f < T(0)) { f += T(1); --k; }
     T a = f;
@@ -386,12 +398,12 @@ __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __res
       const auto A4 = ld4<T>(P.lp + ((size_t)v * P.L + line) * 4);
       const T kf = T(k);
       // x = alpha + sigma*k as (xs, xl)
-      const T qh = A4.z * kf;
+      const T qh = mul_rn(A4.z, kf);
       const T ql = fma(A4.z, kf, -qh);
-      const T xs = A4.x + qh;
-      const T bv = xs - A4.x;
-      const T xe = (A4.x - (xs - bv)) + (qh - bv);
-      const T xl = xe + (A4.y + fma(A4.w, kf, ql));
+      const T xs = add_rn(A4.x, qh);
+      const T bv = sub_rn(xs, A4.x);
+      const T xe = add_rn(sub_rn(A4.x, sub_rn(xs, bv)), sub_rn(qh, bv));
+      const T xl = add_rn(xe, add_rn(A4.y, fma(A4.w, kf, ql)));
       // seed the cell
       const float xf = (float)xs;
       float u = __fdividef(xf * s_inv[j][0], fmaf(xf, s_inv[j][2], s_inv[j][1]));
@@ -402,7 +414,7 @@ __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __res
       while (d > 0 && xs < db2v[2 * d]) --d;
       while (d < D - 1 && db2v[2 * d + 2] <= xs) ++d;
       const T* wdv = P.wd + (size_t)v * D;
-      T a = (xs - db2v[2 * d]) + (xl - db2v[2 * d + 1]);
+      T a = add_rn(sub_rn(xs, db2v[2 * d]), sub_rn(xl, db2v[2 * d + 1]));
       if (a < T(0) && d > 0) { --d; a += wdv[d]; }
       T b = a + (A4.z + A4.w);
       T vacc[SB];
