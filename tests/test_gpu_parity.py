@@ -3,10 +3,12 @@ fixtures, tests/golden/) and against the FP64 oracle.
 
 Tolerances (rel-L2):
 * vs the FP64 oracle: 1e-5 for fp32 data, 1e-12 for fp64 data;
-* vs the reference's fp32 output: 1e-5 on phantom-like inputs; on white-noise
-  sinograms the reference's own fp32 walk is up to ~2e-4 away from fp64
-  (accumulated pixel positions, src/fan_ed_kernel.cu:368-391), so those cases
-  use 3e-4 (same rule as tests/test_oracle_golden.py).
+* vs the reference's fp32 output: 1e-5 on phantom-like inputs (projection,
+  backprojection_t). On white-noise sinograms (projection_t, backprojection)
+  the reference's own fp32 walk drifts from fp64 (accumulated pixel positions,
+  src/fan_ed_kernel.cu:368-391): up to 1.1e-5 on the small fixtures and up to
+  ~1.5e-4 on the 256^2 / 576-view fan fixtures, so those use 3e-5 and 3e-4;
+  fbp, whose ramp filter feeds a high-pass sinogram to that walk, uses 3e-5.
 """
 
 import math
@@ -45,7 +47,7 @@ def _cases():
 def _ref_tol(fname, op):
     if fname.startswith("cfg_fan") and op == "projection_t":
         return 3e-4
-    if fname.startswith("cfg_fan") and op == "fbp":
+    if op in ("projection_t", "backprojection", "fbp"):
         return 3e-5
     return 1e-5
 
