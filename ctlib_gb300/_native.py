@@ -76,6 +76,10 @@ def _declare(l):
         f = getattr(l, name)
         f.argtypes = [vp, vp, vp, c_int, vp, c_size, vp]
         f.restype = c_int
+    l.ctgb_projection_noalloc.argtypes = [vp, vp, vp, c_int, vp]
+    l.ctgb_projection_noalloc.restype = c_int
+    l.ctgb_projection_noalloc_max_bytes.argtypes = []
+    l.ctgb_projection_noalloc_max_bytes.restype = c_size
     l.ctgb_last_error.argtypes = []
     l.ctgb_last_error.restype = ctypes.c_char_p
     l.ctgb_version.restype = c_int
@@ -114,4 +118,5 @@ def check(rc: int, what: str):
 
 EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
-            "ctgb_fbp", "ctgb_last_error", "ctgb_version", "ctgb_geometry_query")
+            "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_last_error",
+            "ctgb_version", "ctgb_geometry_query")

@@ -717,6 +717,57 @@ static int dispatch(const ctgb_plan* p, int op, const void* in, void* out, int b
   return rc;
 }
 
+// ----------------------------------------------------------------------------
+// projection without any allocation
+// ----------------------------------------------------------------------------
+// Scratch for ctgb_projection_noalloc lives in this module's own static device
+// memory instead of a caller-provided buffer. Its size is fixed: every GPU on
+// which this library's kernels are loaded reserves these bytes until process
+// exit. Host code only knows the array through cudaGetSymbolAddress (the name
+// itself is a host-side stand-in, not a device address); the device address is
+// looked up once per device, with that device current, and cached.
+constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;  // 64 MiB
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_dev_ptr[256] = {};
+
+// Device address of the scratch array on `device`, which must be current.
+static int noalloc_scratch(int device, void** out) {
+  if (device < 0 || device >= 256) return fail(CTGB_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_dev_ptr[device]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(CTGB_ERR_CUDA, std::string("scratch symbol address: ") + cudaGetErrorString(e));
+    g_noalloc_dev_ptr[device] = ptr;
+  }
+  *out = g_noalloc_dev_ptr[device];
+  return CTGB_OK;
+}
+
+static int projection_noalloc(const ctgb_plan* p, const void* image, void* sino, int batch, void* stream) {
+  if (!p) return fail(CTGB_ERR_INVALID, "null plan");
+  if (batch <= 0) return batch == 0 ? CTGB_OK : fail(CTGB_ERR_INVALID, "negative batch");
+  const size_t need = workspace_bytes(p, CTGB_OP_PROJECTION, batch);
+  if (need > kNoAllocScratchBytes)
+    return fail(CTGB_ERR_WORKSPACE, "ctgb_projection_noalloc: batch of " + std::to_string(batch) + " needs " +
+                                        std::to_string(need) + " scratch bytes, above the fixed " +
+                                        std::to_string(kNoAllocScratchBytes) +
+                                        "-byte static buffer; use ctgb_projection with a caller workspace");
+  int cur = -1;
+  CTGB_CUDA(cudaGetDevice(&cur));
+  if (cur != p->device) CTGB_CUDA(cudaSetDevice(p->device));
+  void* ws = nullptr;
+  int rc = noalloc_scratch(p->device, &ws);
+  // The layout kernel rewrites every scratch element the gather reads (zero
+  // padding included), so nothing left by an earlier call needs clearing.
+  if (rc == CTGB_OK) rc = dispatch(p, CTGB_OP_PROJECTION, image, sino, batch, ws, kNoAllocScratchBytes, stream);
+  if (cur != p->device && cur >= 0) cudaSetDevice(cur);
+  return rc;
+}
+
 }  // namespace ctgb
 
 // ----------------------------------------------------------------------------
@@ -799,6 +850,12 @@ int ctgb_backprojection_t(const ctgb_plan* p, const void* image, void* sino, int
 int ctgb_fbp(const ctgb_plan* p, const void* sino, void* image, int batch, void* ws, size_t wsb, void* stream) {
   return ctgb::dispatch(p, CTGB_OP_FBP, sino, image, batch, ws, wsb, stream);
 }
+
+int ctgb_projection_noalloc(const ctgb_plan* p, const void* image, void* sino, int batch, void* stream) {
+  return ctgb::projection_noalloc(p, image, sino, batch, stream);
+}
+
+size_t ctgb_projection_noalloc_max_bytes(void) { return ctgb::kNoAllocScratchBytes; }
 
 long ctgb_geometry_query(const double* options, int n_options, int dtype, int what, double* out, size_t n_out) {
   ctgb::HostGeom g;

@@ -94,6 +94,26 @@ int ctgb_backprojection_t(const ctgb_plan* plan, const void* image, void* sino, 
 int ctgb_fbp(const ctgb_plan* plan, const void* sino, void* image, int batch, void* workspace,
              size_t workspace_bytes, void* stream);
 
+/* A (as ctgb_projection) for callers that cannot allocate device memory.
+ * No counterpart in the reference. Some callers of these operators may not
+ * call cudaMalloc, cudaFree or any allocating routine at run time: a C or
+ * embedded host program linked against this library alone has no caching
+ * allocator, where every cudaMalloc/cudaFree can synchronise the device and
+ * stall other streams; a reconstruction service that reserves all of its
+ * device memory at start-up treats a later allocation as a fault. This entry
+ * point takes only the input and output buffers and uses instead a fixed
+ * static scratch array of ctgb_projection_noalloc_max_bytes() bytes (64 MiB)
+ * inside this library, reserved on every GPU that loads it until process exit.
+ * A batch whose scratch (ctgb_workspace_size for CTGB_OP_PROJECTION) exceeds
+ * that size fails with CTGB_ERR_WORKSPACE. The first call on a device looks up
+ * the array's device address; make that first call before any stream capture.
+ * All calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other threads) race on it and must be serialised by the caller. */
+int ctgb_projection_noalloc(const ctgb_plan* plan, const void* image, void* sino, int batch, void* stream);
+
+/* Size in bytes of the static scratch array used by ctgb_projection_noalloc. */
+size_t ctgb_projection_noalloc_max_bytes(void);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* ctgb_last_error(void);
 
