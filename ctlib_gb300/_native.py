@@ -50,8 +50,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return SO_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = SO_PATH + ".tmp"
-    cmd = [nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++17", "-I", INCLUDE, "-Xcompiler", "-fPIC", "-shared",
-           *SOURCES, "-o", tmp]
+    # host code (the plan builder) is compiled without FMA contraction so that
+    # it rounds the same way on x86-64 and aarch64; fused operations it needs
+    # are written as std::fma
+    cmd = [nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++17", "-I", INCLUDE, "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off", "-shared", *SOURCES, "-o", tmp]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     subprocess.run(cmd, check=True)

@@ -65,7 +65,9 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
 
   std::vector<double> cosb(D + 1);
   for (int v = 0; v < V; ++v) {
-    const double ang = (double)((T)v * dAng + Ang0);  // src/fan_ed_kernel.cu:61
+    // idxview * dAng + Ang0 in the data type (src/fan_ed_kernel.cu:61); nvcc's
+    // default FMA contraction makes it one fused multiply-add
+    const double ang = (double)std::fma((T)v, dAng, Ang0);
     const bool xb = std::fabs(ang - std::round(ang / PI) * PI) * 4 / PI <= 1;
     const double e2 = (ang - std::floor(ang / 2 / PI) * 2 * PI) * 4 / PI;
     const bool flip = e2 >= 3 && e2 < 7;

@@ -15,13 +15,18 @@
   harmless because all warps read before any writes, but which a one-thread-at-
   a-time execution would otherwise turn into a real read-after-write.
 
-Both use plain g++ (no cmake, no torch headers); ``-ffp-contract=off`` keeps the
-host results identical on x86-64 and aarch64.
+Both use plain g++ (no cmake, no torch headers). The oracle is built with
+``-ffp-contract=off`` so it rounds identically on x86-64 and aarch64 (the fused
+operations it means are written as std::fma). The reference kernels are built
+with FMA contraction on, as nvcc compiles them by default (--fmad=true), so
+expressions such as ``idxview * *dAng + *Ang0`` become one fused multiply-add
+as on the GPU.
 """
 
 from __future__ import annotations
 
 import os
+import platform
 import re
 import subprocess
 import sys
@@ -97,7 +102,10 @@ def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | No
         parts.append(f.read())
     os.makedirs(REF_DIR, exist_ok=True)
     tmp = REF_SO + ".tmp"
-    subprocess.run(["g++", *CXXFLAGS, "-w", "-I", os.path.join(HERE, "ref_emu"), "-x", "c++", "-",
+    flags = [f for f in CXXFLAGS if f != "-ffp-contract=off"] + ["-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")
+    subprocess.run(["g++", *flags, "-w", "-I", os.path.join(HERE, "ref_emu"), "-x", "c++", "-",
                     "-o", tmp], input="\n".join(parts).encode(), check=True)
     os.replace(tmp, REF_SO)
     return REF_SO

@@ -73,14 +73,13 @@ struct View {
   std::vector<T> cbar;  // fan: mean cosine of the two boundary rays per detector
 };
 
+// View angle idxview * dAng + Ang0 in the data type (src/fan_ed_kernel.cu:61).
+// nvcc's default --fmad=true contracts this expression into one fused
+// multiply-add, so it is evaluated as an FMA here.
 template <class T>
 double view_angle(const Opts<T>& o, int v, bool f32ang) {
-  if (f32ang) {
-    float a = (float)v * (float)o.dAng + (float)o.Ang0;
-    return (double)a;
-  }
-  T a = (T)v * o.dAng + o.Ang0;
-  return (double)a;
+  if (f32ang) return (double)std::fma((float)v, (float)o.dAng, (float)o.Ang0);
+  return (double)std::fma((T)v, o.dAng, o.Ang0);
 }
 
 template <class T>
@@ -456,7 +455,12 @@ int oracle_run(int op, const double* opts, int nopts, int mode, int batch, const
 #endif
   if (mode == 0) return run<float>(op, opts, nopts, true, batch, in, out);
   if (mode == 1) return run<double>(op, opts, nopts, false, batch, in, out);
-  if (mode == 2) return run<double>(op, opts, nopts, true, batch, in, out);
+  if (mode == 2) {
+    // fp32 inputs come with an fp32 options tensor: round the values first
+    std::vector<double> o32(opts, opts + nopts);
+    for (double& x : o32) x = (double)(float)x;
+    return run<double>(op, o32.data(), nopts, true, batch, in, out);
+  }
   return 3;
 }
 
