@@ -22,6 +22,7 @@ from __future__ import annotations
 import torch
 
 from . import _native as N
+from . import tune
 from .ops import _check_input, get_plan
 
 
@@ -35,6 +36,7 @@ def _run(op: int, x: torch.Tensor, plan) -> torch.Tensor:
     out = torch.empty(shape, dtype=x.dtype, device=x.device)
     if B == 0:
         return out
+    tune.apply_cached(plan, op, B)
     with torch.cuda.device(x.device):
         return plan.run(op, x, out)
 

@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
-  const int v = blockIdx.y * 8 + warp;
+  const int v = blockIdx.y * (blockDim.x >> 5) + warp;
   const int g = blockIdx.z;
   if (v >= P.V || d >= P.D) return;
   const int fl = P.flags[v];
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __res
   __shared__ T s_src[kViewChunk][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
-  const int r = blockIdx.y * 8 + warp;
+  const int r = blockIdx.y * (blockDim.x >> 5) + warp;
   const int g = blockIdx.z;
   const bool active = c < P.W && r < P.H;
   const int D = P.D;
@@ -538,6 +538,10 @@ struct ctgb_plan {
   ctgb::HostGeom geom;
   int device = 0;
   int dtype = 0;
+  // per-operator schedule: cap on slices per thread (0 = default) and warps
+  // per CTA of the gather kernel (8 or 4)
+  int sb_cap[5] = {0, 0, 0, 0, 0};
+  int warps[5] = {8, 8, 8, 8, 8};
   void* dev = nullptr;  // one allocation holding all tables
   ctgb::DevPlan<float> pf{};
   ctgb::DevPlan<double> pd{};
@@ -611,9 +615,10 @@ static int upload(ctgb_plan* p) {
   return CTGB_OK;
 }
 
-// slices per thread: float up to 16, double up to 4
-static int slices_per_thread(int dtype, int batch) {
-  const int cap = dtype == 0 ? 16 : 4;
+// slices per thread: float up to 16, double up to 4, or the tuned cap
+static int slices_per_thread(int dtype, int batch, int tuned_cap = 0) {
+  int cap = dtype == 0 ? 16 : 4;
+  if (tuned_cap > 0 && tuned_cap < cap) cap = tuned_cap;
   int sb = 1;
   while (sb < batch && sb < cap) sb *= 2;
   return sb;
@@ -623,7 +628,7 @@ static size_t esize(int dtype) { return dtype == 0 ? 4 : 8; }
 
 static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   const HostGeom& g = p->geom;
-  const int sb = slices_per_thread(p->dtype, batch);
+  const int sb = slices_per_thread(p->dtype, batch, p->sb_cap[op]);
   const size_t G = (size_t)((batch + sb - 1) / sb);
   const size_t es = esize(p->dtype);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -647,11 +652,12 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     const int tb = 256;
     const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
     k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G);
-    dim3 grid((g.D + 31) / 32, (g.V + 7) / 8, G);
+    const int wpc = p->warps[op];
+    dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
     if (op == CTGB_OP_PROJECTION)
-      k_det_gather<T, SB, kA><<<grid, 256, 0, st>>>(P, imx, imy, y, batch);
+      k_det_gather<T, SB, kA><<<grid, 32 * wpc, 0, st>>>(P, imx, imy, y, batch);
     else
-      k_det_gather<T, SB, kBt><<<grid, 256, 0, st>>>(P, imx, imy, y, batch);
+      k_det_gather<T, SB, kBt><<<grid, 32 * wpc, 0, st>>>(P, imx, imy, y, batch);
   } else {
     T* qb = static_cast<T*>(ws);
     if (op == CTGB_OP_FBP) {
@@ -669,13 +675,14 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
       k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr,
                                              batch, g.V, g.D, G);
     }
-    dim3 grid((g.W + 31) / 32, (g.H + 7) / 8, G);
+    const int wpc = p->warps[op];
+    dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
     if (op == CTGB_OP_PROJECTION_T)
-      k_pix_gather<T, SB, kAt><<<grid, 256, 0, st>>>(P, qb, y, batch, T(1), T(1));
+      k_pix_gather<T, SB, kAt><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, T(1), T(1));
     else if (op == CTGB_OP_BACKPROJECTION)
-      k_pix_gather<T, SB, kB><<<grid, 256, 0, st>>>(P, qb, y, batch, T(1), T(1));
+      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, T(1), T(1));
     else
-      k_pix_gather<T, SB, kB><<<grid, 256, 0, st>>>(P, qb, y, batch, P.dAng, T(2));
+      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, P.dAng, T(2));
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -696,7 +703,7 @@ static int dispatch(const ctgb_plan* p, int op, const void* in, void* out, int b
   CTGB_CUDA(cudaGetDevice(&cur));
   if (cur != p->device) CTGB_CUDA(cudaSetDevice(p->device));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int sb = slices_per_thread(p->dtype, batch);
+  const int sb = slices_per_thread(p->dtype, batch, p->sb_cap[op]);
   int rc;
   if (p->dtype == 0) {
     switch (sb) {
@@ -823,6 +830,19 @@ int ctgb_plan_info(const ctgb_plan* p, int* views, int* dets, int* width, int* h
   if (height) *height = p->geom.H;
   if (scan_type) *scan_type = p->geom.scan;
   if (dtype) *dtype = p->dtype;
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int warps_per_cta) {
+  if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
+  if (op < 0 || op > 4) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
+  if (!(slices_per_thread == 0 || slices_per_thread == 1 || slices_per_thread == 2 || slices_per_thread == 4 ||
+        slices_per_thread == 8 || slices_per_thread == 16))
+    return ctgb::fail(CTGB_ERR_INVALID, "slices_per_thread must be 0 (default), 1, 2, 4, 8 or 16");
+  if (!(warps_per_cta == 0 || warps_per_cta == 4 || warps_per_cta == 8))
+    return ctgb::fail(CTGB_ERR_INVALID, "warps_per_cta must be 0 (default), 4 or 8");
+  plan->sb_cap[op] = slices_per_thread;
+  plan->warps[op] = warps_per_cta == 0 ? 8 : warps_per_cta;
   return CTGB_OK;
 }
 

@@ -25,6 +25,7 @@ from collections import OrderedDict
 import torch
 
 from . import _native as N
+from . import tune
 
 _FLOATS = (torch.float32, torch.float64)
 
@@ -172,6 +173,7 @@ def _apply(op: int, x: torch.Tensor, options, name: str) -> torch.Tensor:
         out = torch.empty((B, 1) + img_shape, dtype=x.dtype, device=x.device)
     if B == 0:
         return out
+    tune.apply_cached(plan, op, B)
     with torch.cuda.device(x.device):
         return plan.run(op, x, out)
 

@@ -1,0 +1,118 @@
+"""Autotuner for the operators' launch schedules.
+
+A schedule is (slices carried per thread, warps per CTA) for one operator on one
+plan (`ctgb_plan_set_schedule`). Carrying more slices per thread amortises the
+per-(view, line) geometry over more fused multiply-adds but costs registers
+and therefore resident warps; fewer warps per CTA changes how views (detector
+gather) or image rows (image gather) are grouped for L1 reuse. The best choice
+depends on the geometry, the batch and the GPU, so it is measured: every
+candidate is timed with CUDA events on the caller's device and the fastest is
+kept, in memory and in a JSON cache on disk
+(``$CTLIB_GB300_TUNE_CACHE``, default ``~/.cache/ctlib_gb300/tune.json``).
+
+``ops`` applies a cached schedule automatically; ``tune()`` measures (set
+``CTLIB_GB300_AUTOTUNE=1`` to tune every new (plan, op, batch) on first use).
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+import torch
+
+from . import _native as N
+
+CANDIDATES_F32 = ((16, 8), (16, 4), (8, 8), (8, 4), (4, 8))
+CANDIDATES_F64 = ((4, 8), (4, 4), (2, 8))
+
+_lock = threading.Lock()
+_cache = None
+
+
+def _cache_path() -> str:
+    return os.environ.get("CTLIB_GB300_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "ctlib_gb300", "tune.json"))
+
+
+def _load():
+    global _cache
+    if _cache is None:
+        try:
+            with open(_cache_path()) as f:
+                _cache = json.load(f)
+        except (OSError, ValueError):
+            _cache = {}
+    return _cache
+
+
+def _save():
+    path = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(_cache, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
+def _key(plan, op: int, batch: int) -> str:
+    name = torch.cuda.get_device_name(plan.device)
+    return f"{name}|{plan.dtype}|{op}|{batch}|{','.join(repr(v) for v in plan.values)}"
+
+
+def apply_cached(plan, op: int, batch: int) -> bool:
+    """Set the cached schedule of (plan, op, batch) if there is one."""
+    memo = plan.__dict__.setdefault("_tuned", {})
+    if (op, batch) in memo:
+        return memo[(op, batch)] is not None
+    with _lock:
+        hit = _load().get(_key(plan, op, batch))
+    if hit is not None:
+        N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, int(hit[0]), int(hit[1])), "schedule")
+    elif os.environ.get("CTLIB_GB300_AUTOTUNE") == "1":
+        tune(plan, op, batch)
+        return True
+    memo[(op, batch)] = hit
+    return hit is not None
+
+
+def _inputs(plan, op: int, batch: int):
+    dev = torch.device("cuda", plan.device)
+    img = (batch, 1, plan.height, plan.width)
+    sino = (batch, 1, plan.views, plan.dets)
+    if op in (N.OP_PROJECTION, N.OP_BACKPROJECTION_T):
+        return torch.rand(img, dtype=plan.dtype, device=dev), torch.empty(sino, dtype=plan.dtype, device=dev)
+    return torch.randn(sino, dtype=plan.dtype, device=dev), torch.empty(img, dtype=plan.dtype, device=dev)
+
+
+def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
+    """Time every candidate schedule of `op` for `batch` slices, keep the best."""
+    if candidates is None:
+        candidates = CANDIDATES_F32 if plan.dtype == torch.float32 else CANDIDATES_F64
+    x, out = _inputs(plan, op, batch)
+    stream = torch.cuda.current_stream(x.device)
+    results = []
+    with torch.cuda.device(x.device):
+        for sb, warps in candidates:
+            N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+            plan.run(op, x, out)  # warm-up (and workspace size for this schedule)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                plan.run(op, x, out)
+            b.record(stream)
+            torch.cuda.synchronize(x.device)
+            results.append((a.elapsed_time(b) / reps, sb, warps))
+    results.sort()
+    best_ms, sb, warps = results[0]
+    N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+    with _lock:
+        _load()[_key(plan, op, batch)] = [sb, warps, best_ms]
+        _save()
+    plan.__dict__.setdefault("_tuned", {})[(op, batch)] = [sb, warps]
+    return {"slices_per_thread": sb, "warps_per_cta": warps, "ms": best_ms,
+            "candidates": [{"slices_per_thread": s, "warps_per_cta": w, "ms": m} for m, s, w in results]}

@@ -58,6 +58,14 @@ int ctgb_plan_destroy(ctgb_plan* plan);
 int ctgb_plan_info(const ctgb_plan* plan, int* views, int* dets, int* width, int* height,
                    int* scan_type, int* dtype);
 
+/* Schedule of one operator on a plan, as picked by the autotuner
+ * (ctlib_gb300/tune.py): the largest number of batch slices one thread carries
+ * (1, 2, 4, 8, 16; 0 = default: 16 for fp32, 4 for fp64) and the warps per CTA
+ * of the gather kernel (4 or 8; 0 = default 8). Changes the workspace size.
+ * No counterpart in the reference (its launch shape is fixed, 256 threads per
+ * (slice, view, 256-bin block), src/fan_ed_kernel.cu:1179-1185). */
+int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int warps_per_cta);
+
 /* Scratch bytes `op` needs for `batch` slices (0 is a valid answer). */
 size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch);
 

@@ -1,0 +1,40 @@
+"""Autotuned schedules change only the launch shape: outputs must be identical
+to the default schedule's, bit for bit, and the choice must be cached."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tune_keeps_results_and_caches(tmp_path, monkeypatch):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    monkeypatch.setenv("CTLIB_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    from ctlib_gb300 import _native as N
+    from ctlib_gb300 import ops, tune
+    from ctlib_gb300.workloads import FAN_ED, ellipse_phantom, fan_options
+    monkeypatch.setattr(tune, "_cache", None)
+    opts = fan_options(96, 128, 64, 64, 1.0, 2.0, 0.0, 2 * math.pi / 96, 120.0, 100.0, 0.0, FAN_ED)
+    img = torch.from_numpy(np.stack([ellipse_phantom(64, 64, 1.0, i) for i in range(16)])[:, None]).cuda()
+    o = torch.tensor(opts, dtype=torch.float32)
+    ops.clear_plans()
+    plan = ops.get_plan(o, torch.float32, img.device)
+    ref_a = ops.projection(img, o)
+    ref_at = ops.projection_t(ref_a, o)
+    for op in (N.OP_PROJECTION, N.OP_PROJECTION_T):
+        r = tune.tune(plan, op, img.shape[0], reps=1)
+        assert len(r["candidates"]) >= 3
+    assert os.path.exists(tmp_path / "tune.json")
+    for sb, warps in tune.CANDIDATES_F32:
+        for op in (N.OP_PROJECTION, N.OP_PROJECTION_T):
+            N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+        a = ops.projection(img, o)
+        at = ops.projection_t(a, o)
+        assert torch.equal(a, ref_a), (sb, warps)
+        assert torch.equal(at, ref_at), (sb, warps)
+    ops.clear_plans()
