@@ -85,6 +85,15 @@ def _declare(l):
     l.ctgb_projection_noalloc.restype = c_int
     l.ctgb_projection_noalloc_max_bytes.argtypes = []
     l.ctgb_projection_noalloc_max_bytes.restype = c_size
+    pp = ctypes.POINTER(vp)
+    l.ctgb_ragged_create.argtypes = [ctypes.POINTER(vp), pp, c_int, c_int]
+    l.ctgb_ragged_create.restype = c_int
+    l.ctgb_ragged_destroy.argtypes = [vp]
+    l.ctgb_ragged_destroy.restype = c_int
+    l.ctgb_ragged_workspace_size.argtypes = [vp, c_int]
+    l.ctgb_ragged_workspace_size.restype = c_size
+    l.ctgb_ragged_run.argtypes = [vp, c_int, pp, pp, vp, c_size, vp]
+    l.ctgb_ragged_run.restype = c_int
     l.ctgb_last_error.argtypes = []
     l.ctgb_last_error.restype = ctypes.c_char_p
     l.ctgb_version.restype = c_int
@@ -124,5 +133,6 @@ def check(rc: int, what: str):
 EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_plan_set_schedule",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
-            "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_last_error",
+            "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
+            "ctgb_ragged_destroy", "ctgb_ragged_workspace_size", "ctgb_ragged_run", "ctgb_last_error",
             "ctgb_version", "ctgb_geometry_query")

@@ -1,0 +1,123 @@
+"""Ragged batches: slices with different geometries processed together.
+
+    rb = RaggedBatch([options_0, options_1, ...])      # one options vector per slice
+    sinos = rb.projection([img_0, img_1, ...])          # list of 1 x 1 x V_i x D_i
+    recs = rb.fbp(sinos)                                 # list of 1 x 1 x H_i x W_i
+
+Every stage of an operator is a single persistent launch over all slices
+(``ctgb_ragged_run``): the task list is built once, longest tasks first, and
+per-slice pointers are kernel parameters, so a run can be captured in a CUDA
+graph: ``rb.graphed(op, inputs)`` returns a replayable callable over static
+input/output buffers.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native as N
+from .ops import get_plan
+
+_OPS = {"projection": N.OP_PROJECTION, "projection_t": N.OP_PROJECTION_T, "backprojection": N.OP_BACKPROJECTION,
+        "backprojection_t": N.OP_BACKPROJECTION_T, "fbp": N.OP_FBP}
+
+
+class RaggedBatch:
+    def __init__(self, options_list, device=None):
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        idx = self.device.index if self.device.index is not None else torch.cuda.current_device()
+        self.plans = [get_plan(o, torch.float32, self.device) for o in options_list]
+        n = len(self.plans)
+        arr = (ctypes.c_void_p * n)(*[p.handle.value for p in self.plans])
+        h = ctypes.c_void_p()
+        rc = N.lib().ctgb_ragged_create(ctypes.byref(h), arr, n, idx)
+        N.check(rc, "ragged batch")
+        self.handle = h
+        self.n = n
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            try:
+                N._lib.ctgb_ragged_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def _shapes(self, op):
+        if op in (N.OP_PROJECTION, N.OP_BACKPROJECTION_T):
+            return [(1, 1, p.views, p.dets) for p in self.plans], [(1, 1, p.height, p.width) for p in self.plans]
+        return [(1, 1, p.height, p.width) for p in self.plans], [(1, 1, p.views, p.dets) for p in self.plans]
+
+    def workspace_bytes(self, op: int) -> int:
+        return int(N.lib().ctgb_ragged_workspace_size(self.handle, op))
+
+    def run(self, op, inputs, outputs=None, workspace=None, stream=None):
+        op = _OPS.get(op, op)
+        if len(inputs) != self.n:
+            raise ValueError(f"expected {self.n} slices, got {len(inputs)}")
+        out_shapes, in_shapes = self._shapes(op)
+        for i, (x, shp) in enumerate(zip(inputs, in_shapes)):
+            if not (x.is_cuda and x.is_contiguous() and x.dtype == torch.float32):
+                raise RuntimeError(f"slice {i}: input must be a contiguous float32 CUDA tensor")
+            if tuple(x.shape) != shp and x.numel() != shp[2] * shp[3]:
+                raise ValueError(f"slice {i}: input shape {tuple(x.shape)}, expected {shp}")
+        if outputs is None:
+            outputs = [torch.empty(s, dtype=torch.float32, device=self.device) for s in out_shapes]
+        nbytes = self.workspace_bytes(op)
+        if workspace is None:
+            workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        ins = (ctypes.c_void_p * self.n)(*[x.data_ptr() for x in inputs])
+        outs = (ctypes.c_void_p * self.n)(*[y.data_ptr() for y in outputs])
+        rc = N.lib().ctgb_ragged_run(self.handle, op, ins, outs, workspace.data_ptr(), nbytes, stream.cuda_stream)
+        N.check(rc, "ragged run")
+        return outputs
+
+    def projection(self, images):
+        return self.run(N.OP_PROJECTION, images)
+
+    def projection_t(self, sinos):
+        return self.run(N.OP_PROJECTION_T, sinos)
+
+    def backprojection(self, sinos):
+        return self.run(N.OP_BACKPROJECTION, sinos)
+
+    def backprojection_t(self, images):
+        return self.run(N.OP_BACKPROJECTION_T, images)
+
+    def fbp(self, sinos):
+        return self.run(N.OP_FBP, sinos)
+
+    def graphed(self, ops, inputs):
+        """Capture `ops` (one op name or a chain such as ("projection", "fbp"),
+        each op consuming the previous one's outputs) into a CUDA graph over
+        static copies of `inputs`. Returns (replay, static_inputs, outputs):
+        copy new data into static_inputs, call replay(), read outputs."""
+        if isinstance(ops, str):
+            ops = (ops,)
+        static_in = [x.clone() for x in inputs]
+        bufs, cur = [], static_in
+        for name in ops:
+            op = _OPS[name]
+            out_shapes, _ = self._shapes(op)
+            outs = [torch.empty(s, dtype=torch.float32, device=self.device) for s in out_shapes]
+            ws = torch.empty(max(self.workspace_bytes(op), 1), dtype=torch.uint8, device=self.device)
+            bufs.append((op, cur, outs, ws))
+            cur = outs
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for op, i, o, w in bufs:  # warm-up outside capture
+                self.run(op, i, o, w, stream=side)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for op, i, o, w in bufs:
+                self.run(op, i, o, w)
+        return graph.replay, static_in, cur

@@ -28,6 +28,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -255,14 +256,9 @@ __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
 // anchor k and a fraction f computed from exact products (two-product via FMA),
 // and the cell spans [f, f + w/sigma) pixels from k on.
 template <class T, int SB, int KIND>
-__global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
-                                                    const T* __restrict__ imy, T* __restrict__ out, int B) {
+__device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int d, int g, const T* __restrict__ imx,
+                                                const T* __restrict__ imy, T* __restrict__ out, int B) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int d = blockIdx.x * 32 + lane;
-  const int v = blockIdx.y * (blockDim.x >> 5) + warp;
-  const int g = blockIdx.z;
-  if (v >= P.V || d >= P.D) return;
   const int fl = P.flags[v];
   const bool xb = fl & 1;
   const int nlines = xb ? P.H : P.W;
@@ -346,6 +342,16 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
   }
 }
 
+template <class T, int SB, int KIND>
+__global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
+                                                    const T* __restrict__ imy, T* __restrict__ out, int B) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + lane;
+  const int v = blockIdx.y * (blockDim.x >> 5) + warp;
+  if (v >= P.V || d >= P.D) return;
+  det_gather_cell<T, SB, KIND>(P, v, d, blockIdx.z, imx, imy, out, B);
+}
+
 // ----------------------------------------------------------------------------
 // image gather: A^T (kind kAt) and B (kind kB)
 // ----------------------------------------------------------------------------
@@ -356,17 +362,14 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
 // is taken between the two nearby pairs; the cells then follow by widths.
 constexpr int kViewChunk = 128;
 
+// Called by every thread of the CTA (it synchronises): thread -> pixel (r, c).
 template <class T, int SB, int KIND>
-__global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __restrict__ q, T* __restrict__ img,
-                                                    int B, T out_mul, T out_div) {
+__device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int r, int g, const T* __restrict__ q,
+                                                T* __restrict__ img, int B, T out_mul, T out_div) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   __shared__ float s_inv[kViewChunk][5];
   __shared__ int s_flag[kViewChunk];
   __shared__ T s_src[kViewChunk][2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int c = blockIdx.x * 32 + lane;
-  const int r = blockIdx.y * (blockDim.x >> 5) + warp;
-  const int g = blockIdx.z;
   const bool active = c < P.W && r < P.H;
   const int D = P.D;
   const T* qg = q + (size_t)g * P.V * D * SB;
@@ -464,19 +467,28 @@ __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __res
   }
 }
 
+template <class T, int SB, int KIND>
+__global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __restrict__ q, T* __restrict__ img,
+                                                    int B, T out_mul, T out_div) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  pix_gather_tile<T, SB, KIND>(P, blockIdx.x * 32 + lane, blockIdx.y * (blockDim.x >> 5) + warp, blockIdx.z, q,
+                               img, B, out_mul, out_div);
+}
+
 // ----------------------------------------------------------------------------
 // fbp ramp filter: q[g][v][d][s] = sum_m pre(y)[m] * h[m - k + D - 1], k = ext(d)
 // One CTA per (slice group, view); each thread produces 8 outputs of one parity
 // for one slice: outputs k0, k0+2, ..., k0+14 only meet taps of odd offset (the
 // even non-zero offsets of the RL kernel are zero), plus the centre tap.
 // ----------------------------------------------------------------------------
+// Called by every thread of the CTA; `smem` holds 2D + SB*D elements.
 template <class T, int SB>
-__global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __restrict__ y, T* __restrict__ q,
-                                                     int B) {
-  extern __shared__ unsigned char smem_raw[];
-  T* taps = reinterpret_cast<T*>(smem_raw);          // 2D-1
+__device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int g, const T* __restrict__ y,
+                                                 T* __restrict__ q, int B, T* smem) {
+  T* taps = smem;                                     // 2D-1
   T* rows = taps + (2 * P.D - 1 + 1);                 // SB x D
-  const int v = blockIdx.x, g = blockIdx.y, D = P.D;
+  const int D = P.D;
+  __syncthreads();  // smem may still be read by a previous task of this CTA
   for (int j = threadIdx.x; j < 2 * D - 1; j += blockDim.x) taps[j] = P.taps[j];
   for (int i = threadIdx.x; i < SB * D; i += blockDim.x) {
     const int s = i / D, m = i % D;
@@ -527,6 +539,13 @@ __global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __re
       }
     }
   }
+}
+
+template <class T, int SB>
+__global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __restrict__ y, T* __restrict__ q,
+                                                     int B) {
+  extern __shared__ unsigned char smem_raw[];
+  ramp_filter_view<T, SB>(P, blockIdx.x, blockIdx.y, y, q, B, reinterpret_cast<T*>(smem_raw));
 }
 
 // ----------------------------------------------------------------------------
@@ -725,6 +744,110 @@ static int dispatch(const ctgb_plan* p, int op, const void* in, void* out, int b
 }
 
 // ----------------------------------------------------------------------------
+// ragged batches: slices with their own plans, one persistent launch per stage
+// ----------------------------------------------------------------------------
+// Each stage's work is a host-built task list, longest tasks first; persistent
+// CTAs (as many as fit at once) walk it with a grid stride and read the plan of
+// the task's slice from a device array. Slice pointers travel as a by-value
+// kernel parameter, so a run needs no host-to-device copy and can be captured in
+// a CUDA graph. One slice per plan entry: the gathers run with one slice per
+// thread, and a slice's row lines are its own image (no re-layout needed).
+constexpr int kMaxRagged = 128;
+
+struct RaggedIO {
+  const float* in[kMaxRagged];
+  float* out[kMaxRagged];
+};
+
+struct RTask {
+  int slice, a, b;
+};
+
+__global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<float>* __restrict__ plans,
+                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+                                                       unsigned char* ws, const size_t* __restrict__ off) {
+  __shared__ float tile[32][33];
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const RTask tk = tasks[t];
+    const int H = plans[tk.slice].H, W = plans[tk.slice].W;
+    const float* img = io.in[tk.slice];
+    float* imy = reinterpret_cast<float*>(ws + off[tk.slice]);
+    const int r0 = tk.a * 32, c0 = tk.b * 32;
+    __syncthreads();
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+      const int rr = i >> 5, cc = i & 31, r = r0 + rr, c = c0 + cc;
+      tile[rr][cc] = (r < H && c < W) ? img[(size_t)r * W + c] : 0.f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+      const int cc = i >> 5, rr = i & 31, r = r0 + rr, c = c0 + cc;
+      if (r < H && c < W) imy[(size_t)c * H + (H - 1 - r)] = tile[rr][cc];
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<float>* __restrict__ plans,
+                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+                                                        unsigned char* ws, const size_t* __restrict__ off) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const RTask tk = tasks[t];
+    const DevPlan<float> P = plans[tk.slice];
+    const int v = tk.a * (blockDim.x >> 5) + warp, d = tk.b * 32 + lane;
+    if (v < P.V && d < P.D)
+      det_gather_cell<float, 1, KIND>(P, v, d, 0, io.in[tk.slice],
+                                      reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice], 1);
+  }
+}
+
+template <bool SCALE>
+__global__ void __launch_bounds__(256) k_rag_sino_rows(const DevPlan<float>* __restrict__ plans,
+                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+                                                       unsigned char* ws, const size_t* __restrict__ off) {
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const RTask tk = tasks[t];
+    const DevPlan<float> P = plans[tk.slice];
+    const int v = tk.a, D = P.D;
+    const bool flip = P.flags[v] & 2;
+    const float* y = io.in[tk.slice] + (size_t)v * D;
+    float* q = reinterpret_cast<float*>(ws + off[tk.slice]) + (size_t)v * D;
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+      const float val = y[flip ? D - 1 - d : d];
+      q[d] = SCALE ? val * P.fq[(size_t)v * D + d] : val;
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_rag_pix_gather(const DevPlan<float>* __restrict__ plans,
+                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+                                                        unsigned char* ws, const size_t* __restrict__ off,
+                                                        int fbp_scale) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const RTask tk = tasks[t];
+    const DevPlan<float> P = plans[tk.slice];
+    pix_gather_tile<float, 1, KIND>(P, tk.b * 32 + lane, tk.a * (blockDim.x >> 5) + warp, 0,
+                                    reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice], 1,
+                                    fbp_scale ? P.dAng : 1.f, fbp_scale ? 2.f : 1.f);
+    __syncthreads();  // the next task's view staging reuses shared memory
+  }
+}
+
+__global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<float>* __restrict__ plans,
+                                                  const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+                                                  unsigned char* ws, const size_t* __restrict__ off) {
+  extern __shared__ unsigned char smem_raw[];
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const RTask tk = tasks[t];
+    const DevPlan<float> P = plans[tk.slice];
+    ramp_filter_view<float, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<float*>(ws + off[tk.slice]), 1,
+                               reinterpret_cast<float*>(smem_raw));
+  }
+}
+
+// ----------------------------------------------------------------------------
 // projection without any allocation
 // ----------------------------------------------------------------------------
 // Scratch for ctgb_projection_noalloc lives in this module's own static device
@@ -773,6 +896,153 @@ static int projection_noalloc(const ctgb_plan* p, const void* image, void* sino,
   if (rc == CTGB_OK) rc = dispatch(p, CTGB_OP_PROJECTION, image, sino, batch, ws, kNoAllocScratchBytes, stream);
   if (cur != p->device && cur >= 0) cudaSetDevice(cur);
   return rc;
+}
+
+struct RaggedStage {
+  RTask* tasks = nullptr;  // device
+  int n = 0;
+  int grid = 0;
+};
+
+}  // namespace ctgb
+
+struct ctgb_ragged {
+  int n = 0, device = 0, maxD = 0;
+  void* dev = nullptr;
+  const ctgb::DevPlan<float>* plans = nullptr;
+  const size_t* off_img = nullptr;   // per slice: transposed image in the workspace
+  const size_t* off_sino = nullptr;  // per slice: re-laid-out sinogram in the workspace
+  size_t ws_img = 0, ws_sino = 0;
+  ctgb::RaggedStage transpose, detg, rows, pixg, ramp;
+};
+
+namespace ctgb {
+
+static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
+  int sms = 0;
+  CTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r->device));
+  std::vector<DevPlan<float>> dp(n);
+  std::vector<size_t> oi(n), os(n);
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  std::vector<std::pair<long, RTask>> tr, dg, rw, pg, rp;
+  for (int i = 0; i < n; ++i) {
+    const HostGeom& g = plans[i]->geom;
+    dp[i] = plans[i]->pf;
+    oi[i] = r->ws_img;
+    r->ws_img += al((size_t)g.H * g.W * sizeof(float));
+    os[i] = r->ws_sino;
+    r->ws_sino += al((size_t)g.V * g.D * sizeof(float));
+    if (g.D > r->maxD) r->maxD = g.D;
+    const long lines = g.H > g.W ? g.H : g.W;
+    for (int a = 0; a < (g.H + 31) / 32; ++a)
+      for (int b = 0; b < (g.W + 31) / 32; ++b) tr.push_back({1, {i, a, b}});
+    for (int a = 0; a < (g.V + 7) / 8; ++a)
+      for (int b = 0; b < (g.D + 31) / 32; ++b) dg.push_back({lines, {i, a, b}});
+    for (int a = 0; a < g.V; ++a) {
+      rw.push_back({g.D, {i, a, 0}});
+      rp.push_back({(long)g.D * g.D, {i, a, 0}});
+    }
+    for (int a = 0; a < (g.H + 7) / 8; ++a)
+      for (int b = 0; b < (g.W + 31) / 32; ++b) pg.push_back({g.V, {i, a, b}});
+  }
+  // longest tasks first (stable, so a slice's tasks stay together)
+  for (auto* v : {&tr, &dg, &rw, &pg, &rp})
+    std::stable_sort(v->begin(), v->end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+  const size_t b_plans = al(sizeof(DevPlan<float>) * n), b_off = al(sizeof(size_t) * n);
+  const size_t b_tr = al(sizeof(RTask) * tr.size()), b_dg = al(sizeof(RTask) * dg.size()),
+               b_rw = al(sizeof(RTask) * rw.size()), b_pg = al(sizeof(RTask) * pg.size()),
+               b_rp = al(sizeof(RTask) * rp.size());
+  const size_t total = b_plans + 2 * b_off + b_tr + b_dg + b_rw + b_pg + b_rp;
+  std::vector<unsigned char> host(total, 0);
+  size_t o = 0;
+  auto put = [&](const void* src, size_t bytes, size_t span) {
+    std::memcpy(host.data() + o, src, bytes);
+    const size_t at = o;
+    o += span;
+    return at;
+  };
+  std::vector<RTask> t;
+  const size_t o_plans = put(dp.data(), sizeof(DevPlan<float>) * n, b_plans);
+  const size_t o_oi = put(oi.data(), sizeof(size_t) * n, b_off);
+  const size_t o_os = put(os.data(), sizeof(size_t) * n, b_off);
+  size_t o_stage[5];
+  int cnt[5];
+  int k = 0;
+  for (auto* v : {&tr, &dg, &rw, &pg, &rp}) {
+    t.clear();
+    for (auto& e : *v) t.push_back(e.second);
+    const size_t span = k == 0 ? b_tr : k == 1 ? b_dg : k == 2 ? b_rw : k == 3 ? b_pg : b_rp;
+    o_stage[k] = put(t.data(), sizeof(RTask) * t.size(), span);
+    cnt[k] = (int)t.size();
+    ++k;
+  }
+  CTGB_CUDA(cudaMalloc(&r->dev, total));
+  CTGB_CUDA(cudaMemcpy(r->dev, host.data(), total, cudaMemcpyHostToDevice));
+  unsigned char* base = static_cast<unsigned char*>(r->dev);
+  r->plans = reinterpret_cast<const DevPlan<float>*>(base + o_plans);
+  r->off_img = reinterpret_cast<const size_t*>(base + o_oi);
+  r->off_sino = reinterpret_cast<const size_t*>(base + o_os);
+  RaggedStage* st[5] = {&r->transpose, &r->detg, &r->rows, &r->pixg, &r->ramp};
+  const void* fns[5] = {(const void*)k_rag_transpose, (const void*)k_rag_det_gather<kA>,
+                        (const void*)k_rag_sino_rows<true>, (const void*)k_rag_pix_gather<kAt>,
+                        (const void*)k_rag_ramp};
+  for (int i = 0; i < 5; ++i) {
+    st[i]->tasks = reinterpret_cast<RTask*>(base + o_stage[i]);
+    st[i]->n = cnt[i];
+    int per_sm = 1;
+    const size_t smem = i == 4 ? (size_t)3 * r->maxD * sizeof(float) : 0;
+    CTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 256, smem));
+    const int cap = sms * (per_sm > 0 ? per_sm : 1);
+    st[i]->grid = cnt[i] < cap ? cnt[i] : cap;
+  }
+  return CTGB_OK;
+}
+
+static int ragged_run(const ctgb_ragged* r, int op, const void* const* in, void* const* out, void* ws,
+                      size_t wsb, void* stream) {
+  if (!r) return fail(CTGB_ERR_INVALID, "null ragged batch");
+  if (!in || !out) return fail(CTGB_ERR_INVALID, "null pointer arrays");
+  if (op < 0 || op > 4) return fail(CTGB_ERR_INVALID, "unknown operator");
+  const size_t need = (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) ? r->ws_img : r->ws_sino;
+  if (!ws || wsb < need) return fail(CTGB_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
+  if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) return fail(CTGB_ERR_INVALID, "workspace must be 256-byte aligned");
+  RaggedIO io{};
+  for (int i = 0; i < r->n; ++i) {
+    if (!in[i] || !out[i]) return fail(CTGB_ERR_INVALID, "null slice pointer");
+    io.in[i] = static_cast<const float*>(in[i]);
+    io.out[i] = static_cast<float*>(out[i]);
+  }
+  int cur = -1;
+  CTGB_CUDA(cudaGetDevice(&cur));
+  if (cur != r->device) CTGB_CUDA(cudaSetDevice(r->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
+    k_rag_transpose<<<r->transpose.grid, 256, 0, st>>>(r->plans, r->transpose.tasks, r->transpose.n, io, w,
+                                                       r->off_img);
+    if (op == CTGB_OP_PROJECTION)
+      k_rag_det_gather<kA><<<r->detg.grid, 256, 0, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w, r->off_img);
+    else
+      k_rag_det_gather<kBt><<<r->detg.grid, 256, 0, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w, r->off_img);
+  } else {
+    if (op == CTGB_OP_FBP) {
+      const size_t smem = (size_t)3 * r->maxD * sizeof(float);
+      k_rag_ramp<<<r->ramp.grid, 256, smem, st>>>(r->plans, r->ramp.tasks, r->ramp.n, io, w, r->off_sino);
+    } else if (op == CTGB_OP_PROJECTION_T) {
+      k_rag_sino_rows<true><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
+    } else {
+      k_rag_sino_rows<false><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
+    }
+    if (op == CTGB_OP_PROJECTION_T)
+      k_rag_pix_gather<kAt><<<r->pixg.grid, 256, 0, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w, r->off_sino, 0);
+    else
+      k_rag_pix_gather<kB><<<r->pixg.grid, 256, 0, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w, r->off_sino,
+                                                          op == CTGB_OP_FBP ? 1 : 0);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (cur != r->device && cur >= 0) cudaSetDevice(cur);
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ragged launch: ") + cudaGetErrorString(e));
+  return CTGB_OK;
 }
 
 }  // namespace ctgb
@@ -876,6 +1146,50 @@ int ctgb_projection_noalloc(const ctgb_plan* p, const void* image, void* sino, i
 }
 
 size_t ctgb_projection_noalloc_max_bytes(void) { return ctgb::kNoAllocScratchBytes; }
+
+int ctgb_ragged_create(ctgb_ragged** ragged, const ctgb_plan* const* plans, int n_slices, int device) {
+  if (!ragged || !plans) return ctgb::fail(CTGB_ERR_INVALID, "null pointer");
+  *ragged = nullptr;
+  if (n_slices < 1 || n_slices > ctgb::kMaxRagged)
+    return ctgb::fail(CTGB_ERR_INVALID, "ragged batches hold 1 to " + std::to_string(ctgb::kMaxRagged) + " slices");
+  for (int i = 0; i < n_slices; ++i) {
+    if (!plans[i]) return ctgb::fail(CTGB_ERR_INVALID, "null plan in ragged batch");
+    if (plans[i]->dtype != 0) return ctgb::fail(CTGB_ERR_INVALID, "ragged batches are float32");
+    if (plans[i]->device != device) return ctgb::fail(CTGB_ERR_INVALID, "plan on another device");
+  }
+  auto* r = new ctgb_ragged();
+  r->n = n_slices;
+  r->device = device;
+  int cur = -1;
+  cudaGetDevice(&cur);
+  cudaSetDevice(device);
+  int rc = ctgb::ragged_build(r, plans, n_slices);
+  if (cur >= 0) cudaSetDevice(cur);
+  if (rc != CTGB_OK) {
+    if (r->dev) cudaFree(r->dev);
+    delete r;
+    return rc;
+  }
+  *ragged = r;
+  return CTGB_OK;
+}
+
+int ctgb_ragged_destroy(ctgb_ragged* ragged) {
+  if (!ragged) return CTGB_OK;
+  if (ragged->dev) cudaFree(ragged->dev);
+  delete ragged;
+  return CTGB_OK;
+}
+
+size_t ctgb_ragged_workspace_size(const ctgb_ragged* ragged, int op) {
+  if (!ragged || op < 0 || op > 4) return 0;
+  return (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) ? ragged->ws_img : ragged->ws_sino;
+}
+
+int ctgb_ragged_run(const ctgb_ragged* ragged, int op, const void* const* in, void* const* out, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+  return ctgb::ragged_run(ragged, op, in, out, workspace, workspace_bytes, stream);
+}
 
 long ctgb_geometry_query(const double* options, int n_options, int dtype, int what, double* out, size_t n_out) {
   ctgb::HostGeom g;

@@ -122,6 +122,20 @@ int ctgb_projection_noalloc(const ctgb_plan* plan, const void* image, void* sino
 /* Size in bytes of the static scratch array used by ctgb_projection_noalloc. */
 size_t ctgb_projection_noalloc_max_bytes(void);
 
+/* Ragged batches: n slices (1..128), each with its own fp32 plan (image size,
+ * views, detectors, geometry), processed together: every stage of an operator
+ * is one persistent launch over a task list built here, longest tasks first.
+ * A run takes host arrays of n device pointers (slice i: 1 x 1 x H_i x W_i or
+ * 1 x 1 x V_i x D_i) and needs no host-to-device copy, so it can be captured in
+ * a CUDA graph. The plans must outlive the ragged object. No counterpart in the
+ * reference (one launch per call and geometry, src/ctlib.cpp:15-99). */
+typedef struct ctgb_ragged ctgb_ragged;
+int ctgb_ragged_create(ctgb_ragged** ragged, const ctgb_plan* const* plans, int n_slices, int device);
+int ctgb_ragged_destroy(ctgb_ragged* ragged);
+size_t ctgb_ragged_workspace_size(const ctgb_ragged* ragged, int op);
+int ctgb_ragged_run(const ctgb_ragged* ragged, int op, const void* const* in, void* const* out, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* ctgb_last_error(void);
 
