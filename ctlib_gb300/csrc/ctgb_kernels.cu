@@ -184,14 +184,50 @@ constexpr int kFoldEvery = 16;
 
 
 // ----------------------------------------------------------------------------
+// L2 warm-up of plan tables
+// ----------------------------------------------------------------------------
+// The gathers read per-view / per-line tables with little reuse per CTA; after
+// an L2 flush their first touches go to HBM one dependent load at a time. The
+// layout kernel that runs right before each gather asks the TMA unit to pull
+// those tables into L2 with bulk prefetches of 64 KB (no registers, no smem).
+struct PrefetchList {
+  const void* ptr[6];
+  unsigned long long bytes[6];
+  int n;
+};
+constexpr unsigned kPrefetchChunk = 64u << 10;
+
+__device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// CTA b (thread 0) prefetches chunk b, b + gridDim.x, ... of the concatenated list
+__device__ __forceinline__ void prefetch_tables(const PrefetchList& L) {
+  if (threadIdx.x != 0) return;
+  unsigned long long chunk = 0;
+  for (int t = 0; t < L.n; ++t) {
+    const unsigned long long nb = L.bytes[t];
+    const unsigned long long nch = (nb + kPrefetchChunk - 1) / kPrefetchChunk;
+    for (unsigned long long c = 0; c < nch; ++c, ++chunk) {
+      if (chunk % gridDim.x != blockIdx.x) continue;
+      const unsigned long long off = c * kPrefetchChunk;
+      unsigned len = (unsigned)((nb - off) < kPrefetchChunk ? (nb - off) : kPrefetchChunk);
+      len &= ~15u;  // bulk prefetch sizes are multiples of 16 bytes
+      if (len) l2_prefetch_bulk(static_cast<const unsigned char*>(L.ptr[t]) + off, len);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
 // layout kernels
 // ----------------------------------------------------------------------------
 // image [B][H][W] -> row lines [G][H][NQ][W][QW] and column lines
 // [G][W][NQ][H][QW] (column walk index k = H-1-row), zero-padded to G*SB slices
 template <class T, int SB>
 __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T* __restrict__ imy, int B,
-                               int H, int W, int G) {
+                               int H, int W, int G, PrefetchList pf) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  prefetch_tables(pf);
   const size_t n = (size_t)G * NQ * H * W;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % W);
@@ -213,8 +249,9 @@ __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T
 // (increasing-boundary order), times an optional per-(view, cell) factor
 template <class T, int SB>
 __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const int* __restrict__ flags,
-                              const T* __restrict__ f, int B, int V, int D, int G) {
+                              const T* __restrict__ f, int B, int V, int D, int G, PrefetchList pf) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  prefetch_tables(pf);
   const size_t n = (size_t)G * V * NQ * D;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int d = (int)(i % D);
@@ -277,8 +314,15 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
 #pragma unroll
   for (int s = 0; s < SB; ++s) { sum[s] = T(0); comp[s] = T(0); blk[s] = T(0); }
 
+  auto G4n = ld4<T>(lgv);
+  T sign = lsv[0];
   for (int l = 0; l < nlines; ++l) {
-    const auto G4 = ld4<T>(lgv + 4 * l);
+    const auto G4 = G4n;
+    const T sig = sign;
+    if (l + 1 < nlines) {  // next line's map, loaded while this line is walked
+      G4n = ld4<T>(lgv + 4 * (l + 1));
+      sign = lsv[l + 1];
+    }
     const T ph = mul_rn(Dh, G4.x);
     const T pl = fma(Dh, G4.x, -ph);
     const T corr = add_rn(fma(Dl, G4.x, fma(Dh, G4.y, pl)), G4.w);
@@ -298,7 +342,6 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
       continue;
     }
-    const T sig = lsv[l];
     const T* row = base + (size_t)l * N * SB;
     T lc = T(0);
     if (KIND == kBt && P.scan != kPara) lc = xb ? P.rowc[l] : P.colc[l];
@@ -393,12 +436,17 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
     }
     __syncthreads();
     if (!active) continue;
+    auto lp_of = [&](int jj) {
+      const bool xbj = s_flag[jj] & 1;
+      return ld4<T>(P.lp + ((size_t)(v0 + jj) * P.L + (xbj ? r : c)) * 4);
+    };
+    auto A4n = lp_of(0);
     for (int j = 0; j < nv; ++j) {
       const int v = v0 + j;
       const bool xb = s_flag[j] & 1;
-      const int line = xb ? r : c;
       const int k = xb ? c : P.H - 1 - r;
-      const auto A4 = ld4<T>(P.lp + ((size_t)v * P.L + line) * 4);
+      const auto A4 = A4n;
+      if (j + 1 < nv) A4n = lp_of(j + 1);  // next view's line map, loaded during this view
       const T kf = T(k);
       // x = alpha + sigma*k as (xs, xl)
       const T qh = mul_rn(A4.z, kf);
@@ -670,7 +718,15 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     const size_t n = (size_t)G * g.H * g.W;
     const int tb = 256;
     const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
-    k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G);
+    PrefetchList pf{};
+    const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
+    pf.ptr[0] = P.lg; pf.bytes[0] = VL * 4 * sizeof(T);
+    pf.ptr[1] = P.ls; pf.bytes[1] = VL * sizeof(T);
+    pf.ptr[2] = P.db2; pf.bytes[2] = (VD + g.V) * 2 * sizeof(T);
+    pf.ptr[3] = P.wd; pf.bytes[3] = VD * sizeof(T);
+    pf.ptr[4] = op == CTGB_OP_PROJECTION ? P.fq : P.fbt; pf.bytes[4] = VD * sizeof(T);
+    pf.n = 5;
+    k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G, pf);
     const int wpc = p->warps[op];
     dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
     if (op == CTGB_OP_PROJECTION)
@@ -691,8 +747,14 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
       const size_t n = (size_t)G * g.V * g.D;
       const int tb = 256;
       const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
+      PrefetchList pf{};
+      const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
+      pf.ptr[0] = P.lp; pf.bytes[0] = VL * 4 * sizeof(T);
+      pf.ptr[1] = P.db2; pf.bytes[1] = (VD + g.V) * 2 * sizeof(T);
+      pf.ptr[2] = P.wd; pf.bytes[2] = VD * sizeof(T);
+      pf.n = 3;
       k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr,
-                                             batch, g.V, g.D, G);
+                                             batch, g.V, g.D, G, pf);
     }
     const int wpc = p->warps[op];
     dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
