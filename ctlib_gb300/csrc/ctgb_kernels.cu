@@ -180,6 +180,7 @@ __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)
 
 enum Kind { kA = 0, kBt = 1, kAt = 2, kB = 3 };
 constexpr int kFoldEvery = 16;
+constexpr int kUnroll = 3;  // straight-line pixels per cell / cells per pixel before the remainder loop
 
 
 
@@ -345,31 +346,58 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
     const T* row = base + (size_t)l * N * SB;
     T lc = T(0);
     if (KIND == kBt && P.scan != kPara) lc = xb ? P.rowc[l] : P.colc[l];
-    while (true) {
-      const T ov = (b < T(1) ? b : T(1)) - (a > T(0) ? a : T(0));
-      if (ov > T(0)) {
-        T w = ov;
-        if (KIND == kA) {
-          w *= sig;
-        } else if (P.scan == kFanED) {
-          const T pc = fma(T(k), P.dImg, pc0);
-          w *= xb ? cweight_ed(sx, sy, pc, lc, P.s2r) : cweight_ed(sx, sy, lc, pc, P.s2r);
-        } else if (P.scan == kFanEA) {
-          const T pc = fma(T(k), P.dImg, pc0);
-          w /= xb ? dist2_ea(sx, sy, pc, lc) : dist2_ea(sx, sy, lc, pc);
-        }
-        const T* px = row + (size_t)k * QW;
-#pragma unroll
-        for (int qd = 0; qd < NQ; ++qd) {
-          T u[QW];
-          load_q<T, QW>(px + (size_t)qd * N * QW, u);
-#pragma unroll
-          for (int j = 0; j < QW; ++j) blk[qd * QW + j] = fma(w, u[j], blk[qd * QW + j]);
-        }
+    // weight of pixel k (overlap ov in pixel units)
+    auto weight = [&](T ov, int kk) {
+      T w = ov;
+      if (KIND == kA) {
+        w *= sig;
+      } else if (P.scan == kFanED) {
+        const T pc = fma(T(kk), P.dImg, pc0);
+        w *= xb ? cweight_ed(sx, sy, pc, lc, P.s2r) : cweight_ed(sx, sy, lc, pc, P.s2r);
+      } else if (P.scan == kFanEA) {
+        const T pc = fma(T(kk), P.dImg, pc0);
+        w /= xb ? dist2_ea(sx, sy, pc, lc) : dist2_ea(sx, sy, lc, pc);
       }
-      b -= T(1);
-      if (b <= T(0) || ++k >= N) break;
-      a -= T(1);
+      return w;
+    };
+    // first kUnroll pixels straight-line: all overlaps, then all loads, then
+    // all FMAs (steps past the cell or the image get weight 0 on a clamped,
+    // valid pixel), so the loads of one line are in flight together
+    T wj[kUnroll];
+    int kj[kUnroll];
+#pragma unroll
+    for (int j = 0; j < kUnroll; ++j) {
+      const T aj = a - T(j), bj = b - T(j);
+      T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
+      const bool inside = k + j < N;
+      if (!(ov > T(0)) || !inside) ov = T(0);
+      kj[j] = inside ? k + j : N - 1;
+      wj[j] = ov > T(0) ? weight(ov, kj[j]) : T(0);
+    }
+#pragma unroll
+    for (int qd = 0; qd < NQ; ++qd) {
+      T u[kUnroll][QW];
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) load_q<T, QW>(row + ((size_t)qd * N + kj[j]) * QW, u[j]);
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j)
+#pragma unroll
+        for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(wj[j], u[j][i], blk[qd * QW + i]);
+    }
+    // rare: a cell wider than kUnroll - 1 pixels
+    for (int j = kUnroll; b - T(j) > T(0) && k + j < N; ++j) {
+      const T aj = a - T(j), bj = b - T(j);
+      const T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
+      if (!(ov > T(0))) continue;
+      const T w = weight(ov, k + j);
+      const T* px = row + (size_t)(k + j) * QW;
+#pragma unroll
+      for (int qd = 0; qd < NQ; ++qd) {
+        T u[QW];
+        load_q<T, QW>(px + (size_t)qd * N * QW, u);
+#pragma unroll
+        for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(w, u[i], blk[qd * QW + i]);
+      }
     }
     if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
   }
@@ -474,7 +502,34 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
         for (int s = 0; s < SB; ++s) vacc[s] = T(0);
       }
       const T* qv = qg + (size_t)v * D * SB;
-      while (d < D) {
+      // first kUnroll cells straight-line (cells past the pixel or the detector
+      // get weight 0 on a clamped, valid cell), then the rare remainder
+      T ovj[kUnroll];
+      int dj[kUnroll];
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) {
+        const bool inside = d + j < D;
+        dj[j] = inside ? d + j : D - 1;
+        const T w = wdv[dj[j]];
+        T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+        ovj[j] = (inside && ov > T(0)) ? ov : T(0);
+        a -= w;
+        b -= w;
+      }
+#pragma unroll
+      for (int qd = 0; qd < NQ; ++qd) {
+        T qq[kUnroll][QW];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) load_q<T, QW>(qv + ((size_t)qd * D + dj[j]) * QW, qq[j]);
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j)
+#pragma unroll
+          for (int i = 0; i < QW; ++i) {
+            if (KIND == kAt) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
+            else vacc[qd * QW + i] = fma(ovj[j], qq[j][i], vacc[qd * QW + i]);
+          }
+      }
+      for (d += kUnroll; b > T(0) && d < D; ++d) {
         const T w = wdv[d];
         const T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
         if (ov > T(0)) {
@@ -489,10 +544,8 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
             }
           }
         }
-        b -= w;
-        if (b <= T(0)) break;
         a -= w;
-        ++d;
+        b -= w;
       }
       if (KIND == kB) {
         const T sig = A4.z + A4.w;

@@ -64,20 +64,28 @@ def _key(plan, op: int, batch: int) -> str:
     return f"{name}|{plan.dtype}|{op}|{batch}|{','.join(repr(v) for v in plan.values)}"
 
 
+def _set(plan, op: int, sb: int, warps: int):
+    """Set the plan's schedule for `op` unless it is already the current one
+    (one plan serves every batch size, each with its own tuned schedule)."""
+    cur = plan.__dict__.setdefault("_current", {})
+    if cur.get(op) != (sb, warps):
+        N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+        cur[op] = (sb, warps)
+
+
 def apply_cached(plan, op: int, batch: int) -> bool:
-    """Set the cached schedule of (plan, op, batch) if there is one."""
+    """Use the cached schedule of (plan, op, batch), or the default one."""
     memo = plan.__dict__.setdefault("_tuned", {})
-    if (op, batch) in memo:
-        return memo[(op, batch)] is not None
-    with _lock:
-        hit = _load().get(_key(plan, op, batch))
-    if hit is not None:
-        N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, int(hit[0]), int(hit[1])), "schedule")
-    elif os.environ.get("CTLIB_GB300_AUTOTUNE") == "1":
-        tune(plan, op, batch)
-        return True
-    memo[(op, batch)] = hit
-    return hit is not None
+    if (op, batch) not in memo:
+        with _lock:
+            hit = _load().get(_key(plan, op, batch))
+        if hit is None and os.environ.get("CTLIB_GB300_AUTOTUNE") == "1":
+            tune(plan, op, batch)
+            hit = memo[(op, batch)]
+        memo[(op, batch)] = None if hit is None else (int(hit[0]), int(hit[1]))
+    sched = memo[(op, batch)]
+    _set(plan, op, *(sched if sched is not None else (0, 0)))
+    return sched is not None
 
 
 def _inputs(plan, op: int, batch: int):
@@ -98,7 +106,7 @@ def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
     results = []
     with torch.cuda.device(x.device):
         for sb, warps in candidates:
-            N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+            _set(plan, op, sb, warps)
             plan.run(op, x, out)  # warm-up (and workspace size for this schedule)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -109,10 +117,10 @@ def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
             results.append((a.elapsed_time(b) / reps, sb, warps))
     results.sort()
     best_ms, sb, warps = results[0]
-    N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+    _set(plan, op, sb, warps)
     with _lock:
         _load()[_key(plan, op, batch)] = [sb, warps, best_ms]
         _save()
-    plan.__dict__.setdefault("_tuned", {})[(op, batch)] = [sb, warps]
+    plan.__dict__.setdefault("_tuned", {})[(op, batch)] = (sb, warps)
     return {"slices_per_thread": sb, "warps_per_cta": warps, "ms": best_ms,
             "candidates": [{"slices_per_thread": s, "warps_per_cta": w, "ms": m} for m, s, w in results]}

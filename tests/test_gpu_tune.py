@@ -30,11 +30,16 @@ def test_tune_keeps_results_and_caches(tmp_path, monkeypatch):
         r = tune.tune(plan, op, img.shape[0], reps=1)
         assert len(r["candidates"]) >= 3
     assert os.path.exists(tmp_path / "tune.json")
+    # a schedule tuned for another batch size must not leak into this one
+    tune.tune(plan, N.OP_PROJECTION, 1, reps=1)
+    ops.projection(img, o)
+    assert plan._current[N.OP_PROJECTION] == plan._tuned[(N.OP_PROJECTION, img.shape[0])]
     for sb, warps in tune.CANDIDATES_F32:
         for op in (N.OP_PROJECTION, N.OP_PROJECTION_T):
-            N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
+            plan._tuned[(op, img.shape[0])] = (sb, warps)  # force this schedule for the batch
         a = ops.projection(img, o)
         at = ops.projection_t(a, o)
+        assert plan._current[N.OP_PROJECTION] == (sb, warps)
         assert torch.equal(a, ref_a), (sb, warps)
         assert torch.equal(at, ref_at), (sb, warps)
     ops.clear_plans()
