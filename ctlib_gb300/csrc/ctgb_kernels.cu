@@ -165,6 +165,30 @@ __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
+// Kahan fold of a block partial into a (sum, comp) pair kept in shared memory:
+// the pair is touched once per kFoldEvery lines / views, so it need not hold
+// registers; layout [2][SB][blockDim] keeps the accesses conflict-free.
+template <class T, int SB>
+__device__ __forceinline__ void kahan_fold_smem(T* acc, T (&blk)[SB]) {
+  const int nt = blockDim.x, t = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < SB; ++s) {
+    T* sum = acc + (size_t)s * nt + t;
+    T* comp = acc + (size_t)(SB + s) * nt + t;
+    const T y = sub_rn(blk[s], *comp);
+    const T tt = add_rn(*sum, y);
+    *comp = sub_rn(sub_rn(tt, *sum), y);
+    *sum = tt;
+    blk[s] = T(0);
+  }
+}
+
+template <class T, int SB>
+__device__ __forceinline__ void kahan_init_smem(T* acc) {
+#pragma unroll
+  for (int s = 0; s < 2 * SB; ++s) acc[(size_t)s * blockDim.x + threadIdx.x] = T(0);
+}
+
 // Kahan fold of a block partial into (sum, comp); the partial is reset.
 template <class T, int SB>
 __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)[SB]) {
@@ -311,9 +335,12 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
   if (KIND == kBt && P.scan != kPara) { sx = P.src[2 * v]; sy = P.src[2 * v + 1]; }
   const T pc0 = xb ? P.colc[0] : P.rowc[P.H - 1];  // centre of pixel k = 0 along the walk
 
-  T sum[SB], comp[SB], blk[SB];
+  extern __shared__ unsigned char det_smem[];
+  T* acc = reinterpret_cast<T*>(det_smem);  // [2][SB][blockDim]: running sum, compensation
+  kahan_init_smem<T, SB>(acc);
+  T blk[SB];
 #pragma unroll
-  for (int s = 0; s < SB; ++s) { sum[s] = T(0); comp[s] = T(0); blk[s] = T(0); }
+  for (int s = 0; s < SB; ++s) blk[s] = T(0);
 
   auto G4n = ld4<T>(lgv);
   T sign = lsv[0];
@@ -340,7 +367,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       k = 0;
     }
     if (k >= N || b <= T(0)) {
-      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
+      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
       continue;
     }
     const T* row = base + (size_t)l * N * SB;
@@ -399,9 +426,9 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(w, u[i], blk[qd * QW + i]);
       }
     }
-    if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
+    if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
   }
-  kahan_fold<T, SB>(sum, comp, blk);
+  kahan_fold_smem<T, SB>(acc, blk);
   T fac = T(1);
   if (KIND == kA) fac = P.fq[(size_t)v * P.D + d];
   else if (P.scan == kFanEA) fac = P.fbt[(size_t)v * P.D + d];
@@ -409,7 +436,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
-    if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = sum[s] * fac;
+    if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = acc[(size_t)s * blockDim.x + threadIdx.x] * fac;
   }
 }
 
@@ -448,9 +475,12 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
   const T pcy = active ? P.rowc[r] : T(0);
   const bool ea = P.scan == kFanEA;
 
-  T sum[SB], comp[SB], blk[SB];
+  extern __shared__ unsigned char pix_smem[];
+  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][blockDim]: running sum, compensation
+  kahan_init_smem<T, SB>(acc);
+  T blk[SB];
 #pragma unroll
-  for (int s = 0; s < SB; ++s) { sum[s] = T(0); comp[s] = T(0); blk[s] = T(0); }
+  for (int s = 0; s < SB; ++s) blk[s] = T(0);
 
   for (int v0 = 0; v0 < P.V; v0 += kViewChunk) {
     const int nv = min(kViewChunk, P.V - v0);
@@ -495,11 +525,15 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
       const T* wdv = P.wd + (size_t)v * D;
       T a = add_rn(sub_rn(xs, db2v[2 * d]), sub_rn(xl, db2v[2 * d + 1]));
       if (a < T(0) && d > 0) { --d; a += wdv[d]; }
-      T b = a + (A4.z + A4.w);
-      T vacc[SB];
+      const T sig = A4.z + A4.w;
+      T b = a + sig;
+      // backprojector view weight of this pixel (U^2 / sigma, 1 / (L^2 sigma),
+      // 1 / dImg), folded into each cell's overlap weight
+      T wv = T(1);
       if (KIND == kB) {
-#pragma unroll
-        for (int s = 0; s < SB; ++s) vacc[s] = T(0);
+        if (P.scan == kFanED) wv = cweight_ed(s_src[j][0], s_src[j][1], pcx, pcy, P.s2r) / sig;
+        else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(s_src[j][0], s_src[j][1], pcx, pcy) * sig);
+        else wv = T(1) / P.dImg;
       }
       const T* qv = qg + (size_t)v * D * SB;
       // first kUnroll cells straight-line (cells past the pixel or the detector
@@ -512,7 +546,7 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
         dj[j] = inside ? d + j : D - 1;
         const T w = wdv[dj[j]];
         T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-        ovj[j] = (inside && ov > T(0)) ? ov : T(0);
+        ovj[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
         a -= w;
         b -= w;
       }
@@ -524,47 +558,33 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
 #pragma unroll
         for (int j = 0; j < kUnroll; ++j)
 #pragma unroll
-          for (int i = 0; i < QW; ++i) {
-            if (KIND == kAt) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
-            else vacc[qd * QW + i] = fma(ovj[j], qq[j][i], vacc[qd * QW + i]);
-          }
+          for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
       }
       for (d += kUnroll; b > T(0) && d < D; ++d) {
         const T w = wdv[d];
-        const T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+        T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
         if (ov > T(0)) {
+          if (KIND == kB) ov *= wv;
 #pragma unroll
           for (int qd = 0; qd < NQ; ++qd) {
             T qq[QW];
             load_q<T, QW>(qv + ((size_t)qd * D + d) * QW, qq);
 #pragma unroll
-            for (int i = 0; i < QW; ++i) {
-              if (KIND == kAt) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
-              else vacc[qd * QW + i] = fma(ov, qq[i], vacc[qd * QW + i]);
-            }
+            for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
           }
         }
         a -= w;
         b -= w;
       }
-      if (KIND == kB) {
-        const T sig = A4.z + A4.w;
-        T wv;
-        if (P.scan == kFanED) wv = cweight_ed(s_src[j][0], s_src[j][1], pcx, pcy, P.s2r) / sig;
-        else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(s_src[j][0], s_src[j][1], pcx, pcy) * sig);
-        else wv = T(1) / P.dImg;
-#pragma unroll
-        for (int s = 0; s < SB; ++s) blk[s] = fma(vacc[s], wv, blk[s]);
-      }
-      if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold<T, SB>(sum, comp, blk);
+      if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
     }
   }
   if (!active) return;
-  kahan_fold<T, SB>(sum, comp, blk);
+  kahan_fold_smem<T, SB>(acc, blk);
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
-    if (bb < B) img[((size_t)bb * P.H + r) * P.W + c] = sum[s] * out_mul / out_div;
+    if (bb < B) img[((size_t)bb * P.H + r) * P.W + c] = acc[(size_t)s * blockDim.x + threadIdx.x] * out_mul / out_div;
   }
 }
 
@@ -782,10 +802,11 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G, pf);
     const int wpc = p->warps[op];
     dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
+    const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
     if (op == CTGB_OP_PROJECTION)
-      k_det_gather<T, SB, kA><<<grid, 32 * wpc, 0, st>>>(P, imx, imy, y, batch);
+      k_det_gather<T, SB, kA><<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
     else
-      k_det_gather<T, SB, kBt><<<grid, 32 * wpc, 0, st>>>(P, imx, imy, y, batch);
+      k_det_gather<T, SB, kBt><<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
   } else {
     T* qb = static_cast<T*>(ws);
     if (op == CTGB_OP_FBP) {
@@ -811,12 +832,13 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     }
     const int wpc = p->warps[op];
     dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
+    const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
     if (op == CTGB_OP_PROJECTION_T)
-      k_pix_gather<T, SB, kAt><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, T(1), T(1));
+      k_pix_gather<T, SB, kAt><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, T(1), T(1));
     else if (op == CTGB_OP_BACKPROJECTION)
-      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, T(1), T(1));
+      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, T(1), T(1));
     else
-      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, 0, st>>>(P, qb, y, batch, P.dAng, T(2));
+      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, P.dAng, T(2));
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -1105,7 +1127,8 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     st[i]->tasks = reinterpret_cast<RTask*>(base + o_stage[i]);
     st[i]->n = cnt[i];
     int per_sm = 1;
-    const size_t smem = i == 4 ? (size_t)3 * r->maxD * sizeof(float) : 0;
+    const size_t smem = i == 4 ? (size_t)3 * r->maxD * sizeof(float)
+                               : (i == 1 || i == 3) ? (size_t)2 * 256 * sizeof(float) : 0;
     CTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 256, smem));
     const int cap = sms * (per_sm > 0 ? per_sm : 1);
     st[i]->grid = cnt[i] < cap ? cnt[i] : cap;
@@ -1135,10 +1158,13 @@ static int ragged_run(const ctgb_ragged* r, int op, const void* const* in, void*
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
     k_rag_transpose<<<r->transpose.grid, 256, 0, st>>>(r->plans, r->transpose.tasks, r->transpose.n, io, w,
                                                        r->off_img);
+    const size_t acc_smem = (size_t)2 * 256 * sizeof(float);
     if (op == CTGB_OP_PROJECTION)
-      k_rag_det_gather<kA><<<r->detg.grid, 256, 0, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w, r->off_img);
+      k_rag_det_gather<kA><<<r->detg.grid, 256, acc_smem, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w,
+                                                                r->off_img);
     else
-      k_rag_det_gather<kBt><<<r->detg.grid, 256, 0, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w, r->off_img);
+      k_rag_det_gather<kBt><<<r->detg.grid, 256, acc_smem, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w,
+                                                                 r->off_img);
   } else {
     if (op == CTGB_OP_FBP) {
       const size_t smem = (size_t)3 * r->maxD * sizeof(float);
@@ -1148,11 +1174,13 @@ static int ragged_run(const ctgb_ragged* r, int op, const void* const* in, void*
     } else {
       k_rag_sino_rows<false><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
     }
+    const size_t acc_smem = (size_t)2 * 256 * sizeof(float);
     if (op == CTGB_OP_PROJECTION_T)
-      k_rag_pix_gather<kAt><<<r->pixg.grid, 256, 0, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w, r->off_sino, 0);
+      k_rag_pix_gather<kAt><<<r->pixg.grid, 256, acc_smem, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w,
+                                                                 r->off_sino, 0);
     else
-      k_rag_pix_gather<kB><<<r->pixg.grid, 256, 0, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w, r->off_sino,
-                                                          op == CTGB_OP_FBP ? 1 : 0);
+      k_rag_pix_gather<kB><<<r->pixg.grid, 256, acc_smem, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w,
+                                                                r->off_sino, op == CTGB_OP_FBP ? 1 : 0);
   }
   const cudaError_t e = cudaGetLastError();
   if (cur != r->device && cur >= 0) cudaSetDevice(cur);
