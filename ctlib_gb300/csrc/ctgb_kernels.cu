@@ -629,26 +629,43 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     const int ch = it / (2 * SB);
     const int k0 = ch * 16 + par;
     const T* row = rows + s * D;
-    T acc[8];
+    // blocks of 16 taps are summed plainly (part) and folded into acc with
+    // Kahan compensation (comp): the ramp filter cancels strongly, so the
+    // far, small taps must not be added straight onto the large running sum
+    T acc[8], comp[8], part[8];
     T win[8];
     // window: win[i] = h(m - k0 - 2i) for the current input m (opposite parity)
     int m = 1 - par;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = T(0);
+      comp[i] = T(0);
+      part[i] = T(0);
       const int off = m - k0 - 2 * i;  // odd
       const int ti = off + D - 1;
       win[i] = (ti >= 0 && ti < 2 * D - 1) ? taps[ti] : T(0);
     }
-    for (; m < D; m += 2) {
+    for (int step = 0; m < D; m += 2, ++step) {
       const T xm = row[m];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) acc[i] = fma(xm, win[i], acc[i]);
+      for (int i = 0; i < 8; ++i) part[i] = fma(xm, win[i], part[i]);
 #pragma unroll
       for (int i = 7; i > 0; --i) win[i] = win[i - 1];
       const int ti = m + 2 - k0 + D - 1;
       win[0] = (ti >= 0 && ti < 2 * D - 1) ? taps[ti] : T(0);
+      if ((step & 15) == 15) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const T y = sub_rn(part[i], comp[i]);
+          const T t = add_rn(acc[i], y);
+          comp[i] = sub_rn(sub_rn(t, acc[i]), y);
+          acc[i] = t;
+          part[i] = T(0);
+        }
+      }
     }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = add_rn(acc[i], sub_rn(part[i], comp[i]));
     const T h0 = taps[D - 1];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
