@@ -99,6 +99,8 @@ def _declare(l):
     l.ctgb_version.restype = c_int
     l.ctgb_geometry_query.argtypes = [dptr, c_int, c_int, c_int, dptr, c_size]
     l.ctgb_geometry_query.restype = ctypes.c_long
+    l.ctgb_wait_timeouts.argtypes = [c_int, ctypes.POINTER(ctypes.c_ulonglong), c_int]
+    l.ctgb_wait_timeouts.restype = c_int
     return l
 
 
@@ -135,4 +137,12 @@ EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_pla
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
             "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
             "ctgb_ragged_destroy", "ctgb_ragged_workspace_size", "ctgb_ragged_run", "ctgb_last_error",
-            "ctgb_version", "ctgb_geometry_query")
+            "ctgb_version", "ctgb_geometry_query", "ctgb_wait_timeouts")
+
+
+def wait_timeouts(device: int = 0, reset: bool = False) -> int:
+    """Bounded waits of the staged image gather that ran out on `device`
+    (ctgb_wait_timeouts); 0 unless a copy pipeline stalled."""
+    n = ctypes.c_ulonglong(0)
+    check(lib().ctgb_wait_timeouts(int(device), ctypes.byref(n), int(bool(reset))), "wait counter")
+    return int(n.value)

@@ -72,10 +72,12 @@ static int fail(int code, const std::string& msg) {
 template <class T>
 struct DevPlan {
   int V, D, W, H, L, scan;
+  int Dp;             // D rounded up to a multiple of 4: row stride of cell records and sinogram planes
   T dImg, s2r, dAng, wscale;
   const int* flags;   // V
   const T* src;       // V*2   source x, y
   const T* db2;       // V*(D+1)*2  cell boundaries (hi, lo)
+  const T* rec;       // V*Dp*4 cell records (db hi, db lo, width, next db hi); zero past D
   const T* wd;        // V*D   cell widths
   const T* fq;        // V*D   A / A^T factor
   const T* fbt;       // V*D   EA B^T factor
@@ -87,6 +89,7 @@ struct DevPlan {
   const T* colc;      // W: column centre x
   const T* wpre;      // D
   const T* taps;      // 2D-1
+  const T* tapl;      // 2D-1  fp64 taps minus taps (fp32 plans)
 };
 
 template <class T>
@@ -270,26 +273,32 @@ __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T
   }
 }
 
-// sinogram [B][V][D] (external detector order) -> [G][V][NQ][D][QW]
-// (increasing-boundary order), times an optional per-(view, cell) factor
+// sinogram [B][V][D] (external detector order) -> [G][V][NQ][Dp][QW]
+// (increasing-boundary order, zero past D), times an optional per-(view, cell)
+// factor
 template <class T, int SB>
 __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const int* __restrict__ flags,
-                              const T* __restrict__ f, int B, int V, int D, int G, PrefetchList pf) {
+                              const T* __restrict__ f, int B, int V, int D, int Dp, int G, PrefetchList pf) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   prefetch_tables(pf);
-  const size_t n = (size_t)G * V * NQ * D;
+  const size_t n = (size_t)G * V * NQ * Dp;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int d = (int)(i % D);
-    const int qd = (int)((i / D) % NQ);
-    const int v = (int)((i / ((size_t)D * NQ)) % V);
-    const int g = (int)(i / ((size_t)D * NQ * V));
-    const int de = (flags[v] & 2) ? D - 1 - d : d;
-    const T fac = f ? f[(size_t)v * D + d] : T(1);
+    const int d = (int)(i % Dp);
+    const int qd = (int)((i / Dp) % NQ);
+    const int v = (int)((i / ((size_t)Dp * NQ)) % V);
+    const int g = (int)(i / ((size_t)Dp * NQ * V));
     T val[QW];
+    if (d < D) {
+      const int de = (flags[v] & 2) ? D - 1 - d : d;
+      const T fac = f ? f[(size_t)v * D + d] : T(1);
 #pragma unroll
-    for (int j = 0; j < QW; ++j) {
-      const int b = g * SB + qd * QW + j;
-      val[j] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
+      for (int j = 0; j < QW; ++j) {
+        const int b = g * SB + qd * QW + j;
+        val[j] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < QW; ++j) val[j] = T(0);
     }
     store_q<T, QW>(q + i * QW, val);
   }
@@ -451,6 +460,73 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
 }
 
 // ----------------------------------------------------------------------------
+// mbarrier and bulk-copy primitives (PTX, sm_90 and later)
+// ----------------------------------------------------------------------------
+// Every wait is bounded: after kWaitLimitNs of polling it gives up, the kernel
+// counts the event in g_wait_timeouts and falls back to global loads, so a
+// stalled copy can never hang the GPU.
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+__device__ unsigned long long g_wait_timeouts;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wait for the completion of the phase of parity `parity`; false if it did not
+// complete within the limit
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (unsigned i = 1; i < (1u << 30); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) break;
+  }
+  return false;
+}
+// global -> shared bulk copy (TMA), completion counted in bytes on `bar`;
+// both addresses 16-byte aligned, size a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int& x) { return *reinterpret_cast<const volatile int*>(&x); }
+__device__ __forceinline__ void report_timeout(int* bad) {
+  *reinterpret_cast<volatile int*>(bad) = 1;
+  atomicAdd(&g_wait_timeouts, 1ull);
+}
+
+// ----------------------------------------------------------------------------
 // image gather: A^T (kind kAt) and B (kind kB)
 // ----------------------------------------------------------------------------
 // Thread = pixel (r, c), SB slices, loop over views. Per view the pixel's lower
@@ -458,129 +534,352 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
 // two-sum), its cell d is seeded from the closed-form inverse of the boundary
 // map and corrected against the stored boundaries, and the offset a = x - db[d]
 // is taken between the two nearby pairs; the cells then follow by widths.
-constexpr int kViewChunk = 128;
+//
+// Cells are read through records rec[d] = (db_hi[d], db_lo[d], w[d],
+// db_hi[d+1]) and sinogram planes q[qd][d][QW] with plane stride qs; `rec` and
+// `q` point at cell `base`, and only cells in [dlo, dhi) are read. The same
+// code runs on a shared-memory window of the cells (SM) and on the global
+// tables, with identical arithmetic.
 
-// Called by every thread of the CTA (it synchronises): thread -> pixel (r, c).
-template <class T, int SB, int KIND>
-__device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int r, int g, const T* __restrict__ q,
-                                                T* __restrict__ img, int B, T out_mul, T out_div) {
+template <class T, bool SM>
+__device__ __forceinline__ Quad<T> ldrec(const T* p) {
+  if constexpr (!SM) {
+    return ld4<T>(p);
+  } else if constexpr (sizeof(T) == 4) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    return {a.x, a.y, a.z, a.w};
+  } else {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    return {a.x, a.y, b.x, b.y};
+  }
+}
+
+template <class T, int QW, bool SM>
+__device__ __forceinline__ void ldq(const T* __restrict__ p, T* v) {
+  if constexpr (!SM) {
+    load_q<T, QW>(p, v);
+  } else if constexpr (sizeof(T) == 4 && QW == 4) {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+  } else if constexpr (QW >= 2) {
+    using V2 = typename VecT<T>::v2;
+#pragma unroll
+    for (int i = 0; i < QW / 2; ++i) {
+      const V2 x = reinterpret_cast<const V2*>(p)[i];
+      v[2 * i] = x.x; v[2 * i + 1] = x.y;
+    }
+  } else {
+    v[0] = p[0];
+  }
+}
+
+// fp32 seed of the cell holding axis coordinate x (closed-form inverse of the
+// boundary map), clamped to [dlo, dhi)
+__device__ __forceinline__ int seed_cell(int scan, float xf, const float* inv, int dlo, int dhi) {
+  float u = __fdividef(xf * inv[0], fmaf(xf, inv[2], inv[1]));
+  if (scan == kFanEA) u = atanf(u);
+  const float cb = fmaf(inv[4], u, inv[3]);
+  return (int)fminf(fmaxf(cb, (float)dlo), (float)(dhi - 1));
+}
+
+// one view's contribution to one pixel (lower edge index k on its line, line
+// map A4), accumulated into blk
+template <class T, int SB, int KIND, bool SM>
+__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const float* inv,
+                                         const T* src2, T pcx, T pcy, const T* __restrict__ rec,
+                                         const T* __restrict__ qv, int qs, int base, int dlo, int dhi,
+                                         T (&blk)[SB]) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
-  __shared__ float s_inv[kViewChunk][5];
-  __shared__ int s_flag[kViewChunk];
-  __shared__ T s_src[kViewChunk][2];
+  const T kf = T(k);
+  // x = alpha + sigma*k as (xs, xl)
+  const T qh = mul_rn(A4.z, kf);
+  const T ql = fma(A4.z, kf, -qh);
+  const T xs = add_rn(A4.x, qh);
+  const T bv = sub_rn(xs, A4.x);
+  const T xe = add_rn(sub_rn(A4.x, sub_rn(xs, bv)), sub_rn(qh, bv));
+  const T xl = add_rn(xe, add_rn(A4.y, fma(A4.w, kf, ql)));
+  int d = seed_cell(P.scan, (float)xs, inv, dlo, dhi);
+  while (d > dlo && xs < rec[(size_t)(d - base) * 4]) --d;
+  while (d < dhi - 1 && rec[(size_t)(d - base) * 4 + 3] <= xs) ++d;
+  const Quad<T> rd = ldrec<T, SM>(rec + (size_t)(d - base) * 4);
+  T a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
+  if (a < T(0) && d > dlo) {
+    --d;
+    a += rec[(size_t)(d - base) * 4 + 2];
+  }
+  const T sig = A4.z + A4.w;
+  T b = a + sig;
+  // backprojector view weight of this pixel (U^2 / sigma, 1 / (L^2 sigma),
+  // 1 / dImg), folded into each cell's overlap weight
+  T wv = T(1);
+  if (KIND == kB) {
+    if (P.scan == kFanED) wv = cweight_ed(src2[0], src2[1], pcx, pcy, P.s2r) / sig;
+    else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(src2[0], src2[1], pcx, pcy) * sig);
+    else wv = T(1) / P.dImg;
+  }
+  // first kUnroll cells straight-line (cells past the pixel or the range get
+  // weight 0 on a clamped, valid cell), then the rare remainder
+  T ovj[kUnroll];
+  int dj[kUnroll];
+#pragma unroll
+  for (int j = 0; j < kUnroll; ++j) {
+    const bool inside = d + j < dhi;
+    dj[j] = inside ? d + j : dhi - 1;
+    const T w = rec[(size_t)(dj[j] - base) * 4 + 2];
+    T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+    ovj[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
+    a -= w;
+    b -= w;
+  }
+#pragma unroll
+  for (int qd = 0; qd < NQ; ++qd) {
+    T qq[kUnroll][QW];
+#pragma unroll
+    for (int j = 0; j < kUnroll; ++j) ldq<T, QW, SM>(qv + ((size_t)qd * qs + (dj[j] - base)) * QW, qq[j]);
+#pragma unroll
+    for (int j = 0; j < kUnroll; ++j)
+#pragma unroll
+      for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
+  }
+  for (d += kUnroll; b > T(0) && d < dhi; ++d) {
+    const T w = rec[(size_t)(d - base) * 4 + 2];
+    T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+    if (ov > T(0)) {
+      if (KIND == kB) ov *= wv;
+#pragma unroll
+      for (int qd = 0; qd < NQ; ++qd) {
+        T qq[QW];
+        ldq<T, QW, SM>(qv + ((size_t)qd * qs + (d - base)) * QW, qq);
+#pragma unroll
+        for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
+      }
+    }
+    a -= w;
+    b -= w;
+  }
+}
+
+// view v of pixel (r, c), everything read from the global tables; q planes of
+// view v start at qv with stride qs
+template <class T, int SB, int KIND>
+__device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int r, int c, const T* __restrict__ qv,
+                                                int qs, T pcx, T pcy, T (&blk)[SB]) {
+  const bool xb = P.flags[v] & 1;
+  const int k = xb ? c : P.H - 1 - r;
+  const Quad<T> A4 = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r : c)) * 4);
+  pix_view<T, SB, KIND, false>(P, A4, k, P.inv + (size_t)v * 5, P.src + 2 * v, pcx, pcy,
+                               P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
+}
+
+// Staged image gather. A CTA is a 32 x R pixel tile (R consumer warps, lane =
+// column, warp = row) plus one producer warp. For each view the producer finds
+// the tile's cell footprint from its four corner pixel edges (exact extremes:
+// along a line the edges grow with k, and across lines each edge moves
+// monotonically because the source lies outside the image), and when it fits
+// kWin cells it copies the cell records, the q planes of those cells and the
+// tile's line maps into a ring of kSlots shared-memory slots with TMA bulk
+// copies. Consumers then read only shared memory; a view whose footprint does
+// not fit is read from the global tables instead (same arithmetic, same
+// result). The window carries a margin of two cells on each side, so every cell
+// a pixel can reach (including the seed correction and the step back when the
+// offset is negative) lies inside it.
+constexpr int kWin = 64;   // cells per staged view window (multiple of 4)
+constexpr int kSlots = 8;  // views in flight per CTA
+
+template <class T, int SB>
+struct PixSlot {
+  static constexpr int kQBytes = SB * kWin * (int)sizeof(T);    // NQ planes x kWin cells x QW
+  static constexpr int kRecBytes = kWin * 4 * (int)sizeof(T);   // kWin records
+  static constexpr int kLpBytes = 32 * 4 * (int)sizeof(T);      // up to 32 line maps
+  static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
+};
+
+template <class T, int SB, int KIND>
+__global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
+                                                       T* __restrict__ img, int B, T out_mul, T out_div) {
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  using S = PixSlot<T, SB>;
+  static_assert(NQ + 2 <= 32, "one producer lane per copy");
+  __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
+  __shared__ int s_ws[kSlots], s_fl[kSlots], s_l0[kSlots];
+  __shared__ float s_inv[kSlots][5];
+  __shared__ T s_src[kSlots][2];
+  __shared__ int s_bad;
+  extern __shared__ __align__(16) unsigned char pix_smem[];
+  const int R = (int)(blockDim.x >> 5) - 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][blockDim]: running sum, compensation
+  unsigned char* slots = pix_smem + (size_t)2 * SB * blockDim.x * sizeof(T);
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R, g = blockIdx.z;
+  const int V = P.V, D = P.D, Dp = P.Dp;
+  const T* qg = q + (size_t)g * V * Dp * SB;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kSlots; ++i) {
+      mbar_init(&s_full[i], 1);
+      mbar_init(&s_empty[i], R);
+    }
+    s_bad = 0;
+    mbar_init_fence();
+  }
+  __syncthreads();
+
+  if (warp == R) {  // producer
+    const int c1 = min(c0 + 32, P.W) - 1, r1 = min(r0 + R, P.H) - 1;
+    // Per-view inputs of the window search, loaded for view vb + lane one batch
+    // of 32 views ahead so that their latency overlaps the copies of the batch
+    // before; the search itself (seed, then the bracketing boundaries) costs
+    // one more dependent load, usually without correction steps.
+    struct ViewIn {
+      int fl;
+      float inv[5];
+      T sx, sy;
+      Quad<T> A4[2];
+    };
+    auto load_in = [&](int v, ViewIn& in) {
+      in.fl = 0;
+      if (v >= V) return;
+      in.fl = P.flags[v];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) in.inv[j] = P.inv[(size_t)v * 5 + j];
+      in.sx = P.src[2 * v];
+      in.sy = P.src[2 * v + 1];
+      const bool xb = in.fl & 1;
+      in.A4[0] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r0 : c0)) * 4);
+      in.A4[1] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r1 : c1)) * 4);
+    };
+    // window start of view v, or -1 if the tile's footprint does not fit
+    auto window = [&](int v, const ViewIn& in, int& l0, int& nl) {
+      if (v >= V) return -1;
+      const bool xb = in.fl & 1;
+      int ka, kb;
+      if (xb) { ka = c0; kb = c1 + 1; l0 = r0; nl = r1 - r0 + 1; }
+      else { ka = P.H - 1 - r1; kb = P.H - r0; l0 = c0; nl = c1 - c0 + 1; }
+      const T* db2v = P.db2 + (size_t)v * (D + 1) * 2;
+      T xs[4];
+      int d[4];
+      T lo_b[4], hi_b[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const Quad<T>& A4 = in.A4[e & 1];
+        xs[e] = add_rn(A4.x, mul_rn(A4.z, T((e & 2) ? kb : ka)));
+        d[e] = seed_cell(P.scan, (float)xs[e], in.inv, 0, D);
+        lo_b[e] = db2v[2 * d[e]];
+        hi_b[e] = db2v[2 * d[e] + 2];
+      }
+      int dmin = D, dmax = -1;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        int dd = d[e];
+        if (dd > 0 && xs[e] < lo_b[e]) {
+          do --dd; while (dd > 0 && xs[e] < db2v[2 * dd]);
+        } else if (dd < D - 1 && hi_b[e] <= xs[e]) {
+          do ++dd; while (dd < D - 1 && db2v[2 * dd + 2] <= xs[e]);
+        }
+        dmin = min(dmin, dd);
+        dmax = max(dmax, dd);
+      }
+      const int lo = max(0, dmin - 2) & ~3;
+      const int hi = min(D - 1, dmax + 2);
+      return hi < lo + kWin ? lo : -1;
+    };
+    ViewIn cur, nxt;
+    int ws, l0 = 0, nl = 0;
+    load_in(lane, cur);
+    ws = window(lane, cur, l0, nl);
+    for (int vb = 0; vb < V; vb += 32) {
+      load_in(vb + 32 + lane, nxt);  // in flight during this batch's copies
+      const int nv = min(32, V - vb);
+      for (int j = 0; j < nv; ++j) {
+        const int vj = vb + j, slot = vj % kSlots, use = vj / kSlots;
+        if (lane == 0 && use > 0 && !ld_volatile(s_bad)) {
+          if (!mbar_wait(&s_empty[slot], (use - 1) & 1)) report_timeout(&s_bad);
+        }
+        __syncwarp();
+        const int wsj = __shfl_sync(0xffffffffu, ws, j);
+        const int l0j = __shfl_sync(0xffffffffu, l0, j);
+        const int nlj = __shfl_sync(0xffffffffu, nl, j);
+        const bool staged = wsj >= 0 && !ld_volatile(s_bad);
+        if (lane == j) {
+          s_ws[slot] = staged ? ws : -1;
+          s_fl[slot] = cur.fl;
+          s_l0[slot] = l0;
+#pragma unroll
+          for (int i = 0; i < 5; ++i) s_inv[slot][i] = cur.inv[i];
+          s_src[slot][0] = cur.sx;
+          s_src[slot][1] = cur.sy;
+        }
+        __syncwarp();
+        if (!staged) {
+          if (lane == 0) mbar_arrive(&s_full[slot]);
+          continue;
+        }
+        const int ncell = min(kWin, Dp - wsj);
+        const unsigned qbytes = (unsigned)(ncell * QW * sizeof(T));
+        const unsigned rbytes = (unsigned)(ncell * 4 * sizeof(T));
+        const unsigned lbytes = (unsigned)(nlj * 4 * sizeof(T));
+        if (lane == 0) mbar_arrive_expect_tx(&s_full[slot], NQ * qbytes + rbytes + lbytes);
+        __syncwarp();
+        unsigned char* sl = slots + (size_t)slot * S::kBytes;
+        if (lane < NQ)
+          bulk_g2s(sl + (size_t)lane * kWin * QW * sizeof(T), qg + (((size_t)vj * NQ + lane) * Dp + wsj) * QW,
+                   qbytes, &s_full[slot]);
+        else if (lane == NQ)
+          bulk_g2s(sl + S::kQBytes, P.rec + ((size_t)vj * Dp + wsj) * 4, rbytes, &s_full[slot]);
+        else if (lane == NQ + 1)
+          bulk_g2s(sl + S::kQBytes + S::kRecBytes, P.lp + ((size_t)vj * P.L + l0j) * 4, lbytes, &s_full[slot]);
+      }
+      cur = nxt;
+      ws = window(vb + 32 + lane, cur, l0, nl);
+    }
+    // Normally the consumers have waited on every phase issued. After a wait
+    // ran out, make sure no copy is still landing in this CTA's shared memory.
+    if (lane == 0 && ld_volatile(s_bad)) {
+      for (int i = 0; i < kSlots && i < V; ++i) {
+        const int last = i + ((V - 1 - i) / kSlots) * kSlots;
+        mbar_wait(&s_full[i], (last / kSlots) & 1);
+      }
+    }
+    return;
+  }
+
+  // consumers
+  const int c = c0 + lane, r = r0 + warp;
   const bool active = c < P.W && r < P.H;
-  const int D = P.D;
-  const T* qg = q + (size_t)g * P.V * D * SB;
   const T pcx = active ? P.colc[c] : T(0);
   const T pcy = active ? P.rowc[r] : T(0);
-  const bool ea = P.scan == kFanEA;
-
-  extern __shared__ unsigned char pix_smem[];
-  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][blockDim]: running sum, compensation
   kahan_init_smem<T, SB>(acc);
   T blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) blk[s] = T(0);
-
-  for (int v0 = 0; v0 < P.V; v0 += kViewChunk) {
-    const int nv = min(kViewChunk, P.V - v0);
-    __syncthreads();
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-      s_flag[i] = P.flags[v0 + i];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) s_inv[i][j] = P.inv[(size_t)(v0 + i) * 5 + j];
-      s_src[i][0] = P.src[2 * (v0 + i)];
-      s_src[i][1] = P.src[2 * (v0 + i) + 1];
+  for (int v = 0; v < V; ++v) {
+    const int slot = v % kSlots;
+    bool ok = false;
+    if (!ld_volatile(s_bad)) {
+      ok = mbar_wait(&s_full[slot], (v / kSlots) & 1);
+      if (!ok) report_timeout(&s_bad);
     }
-    __syncthreads();
-    if (!active) continue;
-    auto lp_of = [&](int jj) {
-      const bool xbj = s_flag[jj] & 1;
-      return ld4<T>(P.lp + ((size_t)(v0 + jj) * P.L + (xbj ? r : c)) * 4);
-    };
-    auto A4n = lp_of(0);
-    for (int j = 0; j < nv; ++j) {
-      const int v = v0 + j;
-      const bool xb = s_flag[j] & 1;
-      const int k = xb ? c : P.H - 1 - r;
-      const auto A4 = A4n;
-      if (j + 1 < nv) A4n = lp_of(j + 1);  // next view's line map, loaded during this view
-      const T kf = T(k);
-      // x = alpha + sigma*k as (xs, xl)
-      const T qh = mul_rn(A4.z, kf);
-      const T ql = fma(A4.z, kf, -qh);
-      const T xs = add_rn(A4.x, qh);
-      const T bv = sub_rn(xs, A4.x);
-      const T xe = add_rn(sub_rn(A4.x, sub_rn(xs, bv)), sub_rn(qh, bv));
-      const T xl = add_rn(xe, add_rn(A4.y, fma(A4.w, kf, ql)));
-      // seed the cell
-      const float xf = (float)xs;
-      float u = __fdividef(xf * s_inv[j][0], fmaf(xf, s_inv[j][2], s_inv[j][1]));
-      if (ea) u = atanf(u);
-      const float cb = fmaf(s_inv[j][4], u, s_inv[j][3]);
-      int d = cb < 0.f ? 0 : (cb >= (float)(D - 1) ? D - 1 : (int)cb);
-      const T* db2v = P.db2 + (size_t)v * (D + 1) * 2;
-      while (d > 0 && xs < db2v[2 * d]) --d;
-      while (d < D - 1 && db2v[2 * d + 2] <= xs) ++d;
-      const T* wdv = P.wd + (size_t)v * D;
-      T a = add_rn(sub_rn(xs, db2v[2 * d]), sub_rn(xl, db2v[2 * d + 1]));
-      if (a < T(0) && d > 0) { --d; a += wdv[d]; }
-      const T sig = A4.z + A4.w;
-      T b = a + sig;
-      // backprojector view weight of this pixel (U^2 / sigma, 1 / (L^2 sigma),
-      // 1 / dImg), folded into each cell's overlap weight
-      T wv = T(1);
-      if (KIND == kB) {
-        if (P.scan == kFanED) wv = cweight_ed(s_src[j][0], s_src[j][1], pcx, pcy, P.s2r) / sig;
-        else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(s_src[j][0], s_src[j][1], pcx, pcy) * sig);
-        else wv = T(1) / P.dImg;
+    if (active) {
+      const int ws = ok ? s_ws[slot] : -1;
+      if (ws >= 0) {
+        const bool xb = s_fl[slot] & 1;
+        const unsigned char* sl = slots + (size_t)slot * S::kBytes;
+        const T* sq = reinterpret_cast<const T*>(sl);
+        const T* srec = reinterpret_cast<const T*>(sl + S::kQBytes);
+        const T* slp = reinterpret_cast<const T*>(sl + S::kQBytes + S::kRecBytes);
+        const Quad<T> A4 = ldrec<T, true>(slp + (size_t)((xb ? r : c) - s_l0[slot]) * 4);
+        pix_view<T, SB, KIND, true>(P, A4, xb ? c : P.H - 1 - r, s_inv[slot], s_src[slot], pcx, pcy, srec, sq,
+                                    kWin, ws, ws, min(ws + kWin, D), blk);
+      } else {
+        pix_view_global<T, SB, KIND>(P, v, r, c, qg + (size_t)v * NQ * Dp * QW, Dp, pcx, pcy, blk);
       }
-      const T* qv = qg + (size_t)v * D * SB;
-      // first kUnroll cells straight-line (cells past the pixel or the detector
-      // get weight 0 on a clamped, valid cell), then the rare remainder
-      T ovj[kUnroll];
-      int dj[kUnroll];
-#pragma unroll
-      for (int j = 0; j < kUnroll; ++j) {
-        const bool inside = d + j < D;
-        dj[j] = inside ? d + j : D - 1;
-        const T w = wdv[dj[j]];
-        T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-        ovj[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
-        a -= w;
-        b -= w;
-      }
-#pragma unroll
-      for (int qd = 0; qd < NQ; ++qd) {
-        T qq[kUnroll][QW];
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j) load_q<T, QW>(qv + ((size_t)qd * D + dj[j]) * QW, qq[j]);
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j)
-#pragma unroll
-          for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
-      }
-      for (d += kUnroll; b > T(0) && d < D; ++d) {
-        const T w = wdv[d];
-        T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-        if (ov > T(0)) {
-          if (KIND == kB) ov *= wv;
-#pragma unroll
-          for (int qd = 0; qd < NQ; ++qd) {
-            T qq[QW];
-            load_q<T, QW>(qv + ((size_t)qd * D + d) * QW, qq);
-#pragma unroll
-            for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
-          }
-        }
-        a -= w;
-        b -= w;
-      }
-      if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
     }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&s_empty[slot]);
+    if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
   }
-  if (!active) return;
   kahan_fold_smem<T, SB>(acc, blk);
+  if (!active) return;
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
@@ -588,12 +887,24 @@ __device__ __forceinline__ void pix_gather_tile(const DevPlan<T>& P, int c, int 
   }
 }
 
-template <class T, int SB, int KIND>
-__global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __restrict__ q, T* __restrict__ img,
-                                                    int B, T out_mul, T out_div) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  pix_gather_tile<T, SB, KIND>(P, blockIdx.x * 32 + lane, blockIdx.y * (blockDim.x >> 5) + warp, blockIdx.z, q,
-                               img, B, out_mul, out_div);
+// Unstaged image gather over one pixel per thread, one slice (ragged batches:
+// sinogram rows [V][D], no padding); called by every thread of the CTA.
+template <class T, int KIND>
+__device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int c, int r, const T* __restrict__ q,
+                                                       T* __restrict__ img, T out_mul, T out_div) {
+  extern __shared__ unsigned char pix_smem_g[];
+  T* acc = reinterpret_cast<T*>(pix_smem_g);
+  const bool active = c < P.W && r < P.H;
+  if (!active) return;
+  const T pcx = P.colc[c], pcy = P.rowc[r];
+  kahan_init_smem<T, 1>(acc);
+  T blk[1] = {T(0)};
+  for (int v = 0; v < P.V; ++v) {
+    pix_view_global<T, 1, KIND>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
+    if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk);
+  }
+  kahan_fold_smem<T, 1>(acc, blk);
+  img[(size_t)r * P.W + c] = acc[threadIdx.x] * out_mul / out_div;
 }
 
 // ----------------------------------------------------------------------------
@@ -602,15 +913,21 @@ __global__ void __launch_bounds__(256) k_pix_gather(DevPlan<T> P, const T* __res
 // for one slice: outputs k0, k0+2, ..., k0+14 only meet taps of odd offset (the
 // even non-zero offsets of the RL kernel are zero), plus the centre tap.
 // ----------------------------------------------------------------------------
-// Called by every thread of the CTA; `smem` holds 2D + SB*D elements.
+// Called by every thread of the CTA; `smem` holds 4D + SB*D elements. In fp32
+// the taps are pairs (taps, tapl) and the low parts are summed separately.
 template <class T, int SB>
 __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int g, const T* __restrict__ y,
-                                                 T* __restrict__ q, int B, T* smem) {
-  T* taps = smem;                                     // 2D-1
-  T* rows = taps + (2 * P.D - 1 + 1);                 // SB x D
+                                                 T* __restrict__ q, int qs, int B, T* smem) {
+  constexpr bool kLo = sizeof(T) == 4;
   const int D = P.D;
+  T* taps = smem;              // 2D-1 (+1)
+  T* tapl = taps + 2 * D;      // 2D-1 (+1)
+  T* rows = tapl + 2 * D;      // SB x D
   __syncthreads();  // smem may still be read by a previous task of this CTA
-  for (int j = threadIdx.x; j < 2 * D - 1; j += blockDim.x) taps[j] = P.taps[j];
+  for (int j = threadIdx.x; j < 2 * D - 1; j += blockDim.x) {
+    taps[j] = P.taps[j];
+    tapl[j] = kLo ? P.tapl[j] : T(0);
+  }
   for (int i = threadIdx.x; i < SB * D; i += blockDim.x) {
     const int s = i / D, m = i % D;
     const int bb = g * SB + s;
@@ -622,7 +939,10 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
   const int chunks = (D + 15) / 16;               // 16 outputs (8 per parity) per chunk
   const int items = SB * 2 * chunks;
   const bool flip = P.flags[v] & 2;
-  T* qv = q + ((size_t)g * P.V + v) * D * SB;
+  T* qv = q + ((size_t)g * P.V + v) * qs * SB;
+  for (int i = threadIdx.x; i < SB * (qs - D); i += blockDim.x)  // row padding
+    qv[((size_t)(i / Planes<SB>::QW / (qs - D)) * qs + D + (i / Planes<SB>::QW) % (qs - D)) * Planes<SB>::QW +
+       i % Planes<SB>::QW] = T(0);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     const int s = it % SB;
     const int par = (it / SB) & 1;
@@ -631,9 +951,10 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     const T* row = rows + s * D;
     // blocks of 16 taps are summed plainly (part) and folded into acc with
     // Kahan compensation (comp): the ramp filter cancels strongly, so the
-    // far, small taps must not be added straight onto the large running sum
-    T acc[8], comp[8], part[8];
-    T win[8];
+    // far, small taps must not be added straight onto the large running sum;
+    // the low parts of the taps go to their own plain sum (plo)
+    T acc[8], comp[8], part[8], plo[8];
+    T win[8], wlo[8];
     // window: win[i] = h(m - k0 - 2i) for the current input m (opposite parity)
     int m = 1 - par;
 #pragma unroll
@@ -641,18 +962,30 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
       acc[i] = T(0);
       comp[i] = T(0);
       part[i] = T(0);
+      plo[i] = T(0);
       const int off = m - k0 - 2 * i;  // odd
       const int ti = off + D - 1;
-      win[i] = (ti >= 0 && ti < 2 * D - 1) ? taps[ti] : T(0);
+      const bool ok = ti >= 0 && ti < 2 * D - 1;
+      win[i] = ok ? taps[ti] : T(0);
+      wlo[i] = ok ? tapl[ti] : T(0);
     }
     for (int step = 0; m < D; m += 2, ++step) {
       const T xm = row[m];
 #pragma unroll
       for (int i = 0; i < 8; ++i) part[i] = fma(xm, win[i], part[i]);
+      if constexpr (kLo) {
 #pragma unroll
-      for (int i = 7; i > 0; --i) win[i] = win[i - 1];
+        for (int i = 0; i < 8; ++i) plo[i] = fma(xm, wlo[i], plo[i]);
+      }
+#pragma unroll
+      for (int i = 7; i > 0; --i) {
+        win[i] = win[i - 1];
+        wlo[i] = wlo[i - 1];
+      }
       const int ti = m + 2 - k0 + D - 1;
-      win[0] = (ti >= 0 && ti < 2 * D - 1) ? taps[ti] : T(0);
+      const bool ok = ti >= 0 && ti < 2 * D - 1;
+      win[0] = ok ? taps[ti] : T(0);
+      wlo[0] = ok ? tapl[ti] : T(0);
       if ((step & 15) == 15) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -666,14 +999,15 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[i] = add_rn(acc[i], sub_rn(part[i], comp[i]));
-    const T h0 = taps[D - 1];
+    const T h0 = taps[D - 1], h0l = tapl[D - 1];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int k = k0 + 2 * i;
       if (k < D) {
-        const T val = fma(h0, row[k], acc[i]);
+        T val = fma(h0, row[k], acc[i]);
+        if constexpr (kLo) val = add_rn(val, fma(h0l, row[k], plo[i]));
         const int di = flip ? D - 1 - k : k;
-        qv[((size_t)(s / Planes<SB>::QW) * D + di) * Planes<SB>::QW + (s % Planes<SB>::QW)] = val;
+        qv[((size_t)(s / Planes<SB>::QW) * qs + di) * Planes<SB>::QW + (s % Planes<SB>::QW)] = val;
       }
     }
   }
@@ -683,7 +1017,7 @@ template <class T, int SB>
 __global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __restrict__ y, T* __restrict__ q,
                                                      int B) {
   extern __shared__ unsigned char smem_raw[];
-  ramp_filter_view<T, SB>(P, blockIdx.x, blockIdx.y, y, q, B, reinterpret_cast<T*>(smem_raw));
+  ramp_filter_view<T, SB>(P, blockIdx.x, blockIdx.y, y, q, P.Dp, B, reinterpret_cast<T*>(smem_raw));
 }
 
 // ----------------------------------------------------------------------------
@@ -719,6 +1053,17 @@ static int upload(ctgb_plan* p) {
     db2[2 * i] = hi;
     db2[2 * i + 1] = g.db[i] - hi;
   }
+  const int Dp = (D + 3) & ~3;
+  std::vector<double> rec((size_t)V * Dp * 4, 0.0);
+  for (int v = 0; v < V; ++v)
+    for (int d = 0; d < D; ++d) {
+      double* e = &rec[((size_t)v * Dp + d) * 4];
+      const size_t b = (size_t)v * (D + 1) + d;
+      e[0] = db2[2 * b];
+      e[1] = db2[2 * b + 1];
+      e[2] = g.wd[(size_t)v * D + d];
+      e[3] = db2[2 * b + 2];
+    }
   for (size_t i = 0; i < (size_t)V * L; ++i) {
     const double alpha = g.lp[2 * i], sigma = g.lp[2 * i + 1];
     if (!(sigma > 0)) continue;  // unused line slot (lines = min(H, W) for this view)
@@ -732,7 +1077,7 @@ static int upload(ctgb_plan* p) {
   for (int r = 0; r < g.H; ++r) rowc[r] = (g.height / 2 - r - 0.5) * g.dImg;
   for (int c = 0; c < g.W; ++c) colc[c] = (c - g.width / 2 + 0.5) * g.dImg;
   const std::vector<const std::vector<double>*> tabs = {&g.src, &db2, &g.wd, &g.fq, &g.fbt, &lg, &ls, &lp,
-                                                        &rowc, &colc, &g.wpre, &g.taps};
+                                                        &rowc, &colc, &g.wpre, &g.taps, &g.taps_lo, &rec};
   size_t off = 0;
   std::vector<size_t> offs;
   auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -766,6 +1111,9 @@ static int upload(ctgb_plan* p) {
   P.colc = reinterpret_cast<const T*>(b + offs[9]);
   P.wpre = reinterpret_cast<const T*>(b + offs[10]);
   P.taps = reinterpret_cast<const T*>(b + offs[11]);
+  P.tapl = reinterpret_cast<const T*>(b + offs[12]);
+  P.rec = reinterpret_cast<const T*>(b + offs[13]);
+  P.Dp = Dp;
   P.flags = reinterpret_cast<const int*>(b + off_flags);
   P.inv = reinterpret_cast<const float*>(b + off_inv);
   if constexpr (sizeof(T) == 4) p->pf = P; else p->pd = P;
@@ -791,7 +1139,7 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
     return 2 * al(G * g.H * g.W * sb * es);
-  return al(G * g.V * g.D * sb * es);
+  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
 }
 
 template <class T, int SB>
@@ -827,7 +1175,7 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
   } else {
     T* qb = static_cast<T*>(ws);
     if (op == CTGB_OP_FBP) {
-      const size_t smem = ((size_t)2 * g.D + (size_t)SB * g.D) * sizeof(T);
+      const size_t smem = ((size_t)4 * g.D + (size_t)SB * g.D) * sizeof(T);
       if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_ramp_filter<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
@@ -835,27 +1183,33 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
       }
       k_ramp_filter<T, SB><<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
     } else {
-      const size_t n = (size_t)G * g.V * g.D;
+      const size_t n = (size_t)G * g.V * P.Dp;
       const int tb = 256;
       const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
       PrefetchList pf{};
-      const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
+      const size_t VL = (size_t)g.V * g.L;
       pf.ptr[0] = P.lp; pf.bytes[0] = VL * 4 * sizeof(T);
-      pf.ptr[1] = P.db2; pf.bytes[1] = (VD + g.V) * 2 * sizeof(T);
-      pf.ptr[2] = P.wd; pf.bytes[2] = VD * sizeof(T);
+      pf.ptr[1] = P.rec; pf.bytes[1] = (size_t)g.V * P.Dp * 4 * sizeof(T);
+      pf.ptr[2] = P.db2; pf.bytes[2] = ((size_t)g.V * g.D + g.V) * 2 * sizeof(T);
       pf.n = 3;
       k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr,
-                                             batch, g.V, g.D, G, pf);
+                                             batch, g.V, g.D, P.Dp, G, pf);
     }
-    const int wpc = p->warps[op];
+    const int wpc = p->warps[op];  // consumer warps (one pixel row each) + one producer warp
     dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
-    const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
-    if (op == CTGB_OP_PROJECTION_T)
-      k_pix_gather<T, SB, kAt><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, T(1), T(1));
-    else if (op == CTGB_OP_BACKPROJECTION)
-      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, T(1), T(1));
-    else
-      k_pix_gather<T, SB, kB><<<grid, 32 * wpc, acc_smem, st>>>(P, qb, y, batch, P.dAng, T(2));
+    const int nt = 32 * (wpc + 1);
+    const size_t smem = (size_t)2 * SB * nt * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
+    auto launch = [&](auto kern, T mul, T div) -> int {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
+      kern<<<grid, nt, smem, st>>>(P, qb, y, batch, mul, div);
+      return CTGB_OK;
+    };
+    int rc;
+    if (op == CTGB_OP_PROJECTION_T) rc = launch(k_pix_gather<T, SB, kAt>, T(1), T(1));
+    else if (op == CTGB_OP_BACKPROJECTION) rc = launch(k_pix_gather<T, SB, kB>, T(1), T(1));
+    else rc = launch(k_pix_gather<T, SB, kB>, P.dAng, T(2));
+    if (rc != CTGB_OK) return rc;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -982,9 +1336,9 @@ __global__ void __launch_bounds__(256) k_rag_pix_gather(const DevPlan<float>* __
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
     const DevPlan<float> P = plans[tk.slice];
-    pix_gather_tile<float, 1, KIND>(P, tk.b * 32 + lane, tk.a * (blockDim.x >> 5) + warp, 0,
-                                    reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice], 1,
-                                    fbp_scale ? P.dAng : 1.f, fbp_scale ? 2.f : 1.f);
+    pix_gather_tile_global<float, KIND>(P, tk.b * 32 + lane, tk.a * (blockDim.x >> 5) + warp,
+                                        reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice],
+                                        fbp_scale ? P.dAng : 1.f, fbp_scale ? 2.f : 1.f);
     __syncthreads();  // the next task's view staging reuses shared memory
   }
 }
@@ -996,8 +1350,8 @@ __global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<float>* __restri
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
     const DevPlan<float> P = plans[tk.slice];
-    ramp_filter_view<float, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<float*>(ws + off[tk.slice]), 1,
-                               reinterpret_cast<float*>(smem_raw));
+    ramp_filter_view<float, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<float*>(ws + off[tk.slice]), P.D,
+                               1, reinterpret_cast<float*>(smem_raw));
   }
 }
 
@@ -1144,7 +1498,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     st[i]->tasks = reinterpret_cast<RTask*>(base + o_stage[i]);
     st[i]->n = cnt[i];
     int per_sm = 1;
-    const size_t smem = i == 4 ? (size_t)3 * r->maxD * sizeof(float)
+    const size_t smem = i == 4 ? (size_t)5 * r->maxD * sizeof(float)
                                : (i == 1 || i == 3) ? (size_t)2 * 256 * sizeof(float) : 0;
     CTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 256, smem));
     const int cap = sms * (per_sm > 0 ? per_sm : 1);
@@ -1184,7 +1538,7 @@ static int ragged_run(const ctgb_ragged* r, int op, const void* const* in, void*
                                                                  r->off_img);
   } else {
     if (op == CTGB_OP_FBP) {
-      const size_t smem = (size_t)3 * r->maxD * sizeof(float);
+      const size_t smem = (size_t)5 * r->maxD * sizeof(float);
       k_rag_ramp<<<r->ramp.grid, 256, smem, st>>>(r->plans, r->ramp.tasks, r->ramp.n, io, w, r->off_sino);
     } else if (op == CTGB_OP_PROJECTION_T) {
       k_rag_sino_rows<true><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
@@ -1215,6 +1569,22 @@ extern "C" {
 int ctgb_version(void) { return 1; }
 
 const char* ctgb_last_error(void) { return ctgb::g_err.c_str(); }
+
+int ctgb_wait_timeouts(int device, unsigned long long* count, int reset) {
+  using namespace ctgb;
+  if (!count) return fail(CTGB_ERR_INVALID, "null count");
+  int cur = -1;
+  CTGB_CUDA(cudaGetDevice(&cur));
+  if (cur != device) CTGB_CUDA(cudaSetDevice(device));
+  cudaError_t e = cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(unsigned long long));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long zero = 0;
+    e = cudaMemcpyToSymbol(g_wait_timeouts, &zero, sizeof(zero));
+  }
+  if (cur != device && cur >= 0) cudaSetDevice(cur);
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("wait counter: ") + cudaGetErrorString(e));
+  return CTGB_OK;
+}
 
 int ctgb_plan_create(ctgb_plan** plan, const double* options, int n_options, int dtype, int device) {
   using namespace ctgb;

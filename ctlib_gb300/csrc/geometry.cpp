@@ -190,13 +190,24 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
   } else {
     for (int k = 0; k < D; ++k) g.wpre[k] = (double)dDet;
   }
+  // The taps are the reference's values in T. In fp32 the filter also applies
+  // the remainder to the fp64 taps: the RL kernel's response nearly cancels on
+  // smooth rows, so the fp32 rounding of the taps alone moves an equal-angle
+  // reconstruction by ~1e-5 relative.
   g.taps.assign(2 * D - 1, 0.0);
+  g.taps_lo.assign(2 * D - 1, 0.0);
+  const double df = (double)dfilt;
   for (int j = 0; j < 2 * D - 1; ++j) {
     const int x = j - D + 1;
-    if (std::abs(x) % 2 == 1)
-      g.taps[j] = (double)(T)(-1 / (PI * PI * x * x * (double)dfilt * (double)dfilt));
-    else if (x == 0)
+    double exact = 0.0;
+    if (std::abs(x) % 2 == 1) {
+      exact = -1 / (PI * PI * x * x * df * df);
+      g.taps[j] = (double)(T)exact;
+    } else if (x == 0) {
+      exact = 1 / (4 * df * df);
       g.taps[j] = (double)(T)(1 / (4 * dfilt * dfilt));
+    }
+    if (sizeof(T) == 4) g.taps_lo[j] = exact - g.taps[j];
   }
   return true;
 }

@@ -40,6 +40,7 @@ struct HostGeom {
   std::vector<double> wpre;    // D: fbp detector pre-weight, applied as (y * wpre[k]) * wscale
   double wscale = 1.0;
   std::vector<double> taps;    // 2D-1: RL ramp taps (src/fan_ed_kernel.cu:926-943)
+  std::vector<double> taps_lo; // 2D-1: fp64 tap minus the stored one (fp32 plans), else 0
   double x0 = 0, y0 = 0;       // left image edge x, bottom image edge y
 };
 

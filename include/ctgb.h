@@ -139,6 +139,14 @@ int ctgb_ragged_run(const ctgb_ragged* ragged, int op, const void* const* in, vo
 /* Message of the last failed call on this thread ("" if none). */
 const char* ctgb_last_error(void);
 
+/* Number of bounded waits in the staged image gather (A^T, B, fbp) that ran out
+ * on `device` since the library was loaded or last reset (`reset` != 0 zeroes
+ * it after reading). Each such event makes the affected CTA finish on global
+ * loads, so results stay correct; a non-zero count means a copy pipeline stalled
+ * for over a second. Synchronises the device. Diagnostics only: no counterpart
+ * in the reference. */
+int ctgb_wait_timeouts(int device, unsigned long long* count, int reset);
+
 /* ABI version, bumped on incompatible changes. */
 int ctgb_version(void);
 

@@ -155,3 +155,35 @@ def test_options_on_gpu_and_channels(ct, oracle_mod):
     got = ct.projection(torch.from_numpy(img).cuda(), torch.tensor(opts, device="cuda")).cpu().numpy()
     want = O.run("projection", np.ascontiguousarray(img[:, :1]), opts, O.MODE_F64_ON_F32)
     assert O.rel_l2(got, want) <= 1e-5
+
+
+def _fine_geom(scan):
+    # 96 x 72 pixels of 1 mm over 1.5-2 detector cells per pixel: the 32-pixel
+    # wide tiles of the image gather span 50-110 cells depending on the view
+    from ctlib_gb300.workloads import fan_options, para_options, FAN_ED, FAN_EA
+    if scan == 0:
+        return fan_options(60, 200, 96, 72, 1.0, 1.0, 0.2, 2 * math.pi / 60, 120.0, 100.0, 0.3, FAN_ED)
+    if scan == 1:
+        return fan_options(60, 200, 96, 72, 1.0, 0.0055, 0.2, 2 * math.pi / 60, 120.0, 100.0, 0.3 * 0.0055, FAN_EA)
+    return para_options(60, 240, 96, 72, 1.0, 0.5, 0.2, math.pi / 60, 0.3)
+
+
+@pytest.mark.parametrize("scan", [0, 1, 2])
+@pytest.mark.parametrize("batch", [5, 16])
+def test_image_gather_staged_and_global_views(ct, oracle_mod, scan, batch):
+    """The image gather (projection_t, backprojection, fbp) copies each view's
+    cell window into shared memory when the tile footprint fits 64 cells and
+    reads the global tables otherwise. These geometries mix both kinds of views
+    within one launch; the result must match the FP64 oracle either way, and no
+    bounded wait of the copy pipeline may have run out."""
+    from ctlib_gb300 import _native
+    O = oracle_mod
+    opts = _fine_geom(scan)
+    rng = np.random.default_rng(100 + 10 * scan + batch)
+    sino = rng.standard_normal((batch, 1, 60, int(opts[1]))).astype(np.float32)
+    before = _native.wait_timeouts(0)
+    for op in ("projection_t", "backprojection", "fbp"):
+        got = _run(ct, op, sino, opts)
+        want = O.run(op, sino, opts, O.MODE_F64_ON_F32)
+        assert O.rel_l2(got, want) <= 1e-5, (op, O.rel_l2(got, want))
+    assert _native.wait_timeouts(0) == before
