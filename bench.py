@@ -198,7 +198,8 @@ def run_ours(args):
         from ctlib_gb300 import _native as N
         for op, name in ((N.OP_PROJECTION, "projection"), (N.OP_PROJECTION_T, "projection_t")):
             r = tune.tune(plan, op, B)
-            tuned[name] = {"slices_per_thread": r["slices_per_thread"], "warps_per_cta": r["warps_per_cta"]}
+            tuned[name] = {"slices_per_thread": r["slices_per_thread"], "warps_per_cta": r["warps_per_cta"],
+                           "unroll": r["unroll"]}
             tune.tune(plan, op, 1)  # schedule of the one-slice-per-call path
     # warm-up (builds plans, workspace, caches)
     for _ in range(args.warmup):

@@ -207,7 +207,8 @@ __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)
 
 enum Kind { kA = 0, kBt = 1, kAt = 2, kB = 3 };
 constexpr int kFoldEvery = 16;
-constexpr int kUnroll = 3;  // straight-line pixels per cell / cells per pixel before the remainder loop
+// Straight-line pixels per cell (cells per pixel) before the remainder loop: U
+// = 3 or 2 per operator (ctgb_plan_set_unroll), 3 unless tuned.
 
 
 
@@ -326,7 +327,7 @@ __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
 // pixel-edge units is u = db*(1/sigma) + beta; it is split into an integer
 // anchor k and a fraction f computed from exact products (two-product via FMA),
 // and the cell spans [f, f + w/sigma) pixels from k on.
-template <class T, int SB, int KIND>
+template <class T, int SB, int KIND, int U>
 __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int d, int g, const T* __restrict__ imx,
                                                 const T* __restrict__ imy, T* __restrict__ out, int B) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
@@ -396,13 +397,13 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       }
       return w;
     };
-    // first kUnroll pixels straight-line: all overlaps, then all loads, then
+    // first U pixels straight-line: all overlaps, then all loads, then
     // all FMAs (steps past the cell or the image get weight 0 on a clamped,
     // valid pixel), so the loads of one line are in flight together
-    T wj[kUnroll];
-    int kj[kUnroll];
+    T wj[U];
+    int kj[U];
 #pragma unroll
-    for (int j = 0; j < kUnroll; ++j) {
+    for (int j = 0; j < U; ++j) {
       const T aj = a - T(j), bj = b - T(j);
       T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
       const bool inside = k + j < N;
@@ -412,16 +413,16 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
     }
 #pragma unroll
     for (int qd = 0; qd < NQ; ++qd) {
-      T u[kUnroll][QW];
+      T u[U][QW];
 #pragma unroll
-      for (int j = 0; j < kUnroll; ++j) load_q<T, QW>(row + ((size_t)qd * N + kj[j]) * QW, u[j]);
+      for (int j = 0; j < U; ++j) load_q<T, QW>(row + ((size_t)qd * N + kj[j]) * QW, u[j]);
 #pragma unroll
-      for (int j = 0; j < kUnroll; ++j)
+      for (int j = 0; j < U; ++j)
 #pragma unroll
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(wj[j], u[j][i], blk[qd * QW + i]);
     }
-    // rare: a cell wider than kUnroll - 1 pixels
-    for (int j = kUnroll; b - T(j) > T(0) && k + j < N; ++j) {
+    // rare: a cell wider than U - 1 pixels
+    for (int j = U; b - T(j) > T(0) && k + j < N; ++j) {
       const T aj = a - T(j), bj = b - T(j);
       const T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
       if (!(ov > T(0))) continue;
@@ -449,14 +450,14 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
   }
 }
 
-template <class T, int SB, int KIND>
+template <class T, int SB, int KIND, int U>
 __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
                                                     const T* __restrict__ imy, T* __restrict__ out, int B) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
   const int v = blockIdx.y * (blockDim.x >> 5) + warp;
   if (v >= P.V || d >= P.D) return;
-  det_gather_cell<T, SB, KIND>(P, v, d, blockIdx.z, imx, imy, out, B);
+  det_gather_cell<T, SB, KIND, U>(P, v, d, blockIdx.z, imx, imy, out, B);
 }
 
 // ----------------------------------------------------------------------------
@@ -574,22 +575,27 @@ __device__ __forceinline__ void ldq(const T* __restrict__ p, T* v) {
   }
 }
 
-// fp32 seed of the cell holding axis coordinate x (closed-form inverse of the
-// boundary map), clamped to [dlo, dhi)
-__device__ __forceinline__ int seed_cell(int scan, float xf, const float* inv, int dlo, int dhi) {
-  float u = __fdividef(xf * inv[0], fmaf(xf, inv[2], inv[1]));
+// Per-view constants of the closed-form inverse of the boundary map:
+// u = x*a / (x*c + b) (atan'ed for equal-angle fans), cell = e*u + d.
+struct Seed {
+  float a, b, c, d, e;
+};
+__device__ __forceinline__ Seed load_seed(const float* p) { return {p[0], p[1], p[2], p[3], p[4]}; }
+
+// fp32 seed of the cell holding axis coordinate x, clamped to [dlo, dhi)
+__device__ __forceinline__ int seed_cell(int scan, float xf, const Seed& sd, int dlo, int dhi) {
+  float u = __fdividef(xf * sd.a, fmaf(xf, sd.c, sd.b));
   if (scan == kFanEA) u = atanf(u);
-  const float cb = fmaf(inv[4], u, inv[3]);
+  const float cb = fmaf(sd.e, u, sd.d);
   return (int)fminf(fmaxf(cb, (float)dlo), (float)(dhi - 1));
 }
 
 // one view's contribution to one pixel (lower edge index k on its line, line
-// map A4), accumulated into blk
-template <class T, int SB, int KIND, bool SM>
-__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const float* inv,
-                                         const T* src2, T pcx, T pcy, const T* __restrict__ rec,
-                                         const T* __restrict__ qv, int qs, int base, int dlo, int dhi,
-                                         T (&blk)[SB]) {
+// map A4), accumulated into blk; U cells straight-line, then the remainder
+template <class T, int SB, int KIND, int U, bool SM>
+__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
+                                         T pcx, T pcy, const T* __restrict__ rec, const T* __restrict__ qv, int qs,
+                                         int base, int dlo, int dhi, T (&blk)[SB]) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   const T kf = T(k);
   // x = alpha + sigma*k as (xs, xl)
@@ -599,14 +605,27 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
   const T bv = sub_rn(xs, A4.x);
   const T xe = add_rn(sub_rn(A4.x, sub_rn(xs, bv)), sub_rn(qh, bv));
   const T xl = add_rn(xe, add_rn(A4.y, fma(A4.w, kf, ql)));
-  int d = seed_cell(P.scan, (float)xs, inv, dlo, dhi);
-  while (d > dlo && xs < rec[(size_t)(d - base) * 4]) --d;
-  while (d < dhi - 1 && rec[(size_t)(d - base) * 4 + 3] <= xs) ++d;
-  const Quad<T> rd = ldrec<T, SM>(rec + (size_t)(d - base) * 4);
+  // seed the cell and correct it: db_hi[d] <= xs < db_hi[d+1], d in [dlo, dhi)
+  int d = seed_cell(P.scan, (float)xs, sd, dlo, dhi);
+  Quad<T> rd = ldrec<T, SM>(rec + (d - base) * 4);
+  if (d > dlo && xs < rd.x) {
+    do {
+      --d;
+      rd = ldrec<T, SM>(rec + (d - base) * 4);
+    } while (d > dlo && xs < rd.x);
+  } else if (d < dhi - 1 && rd.w <= xs) {
+    do {
+      ++d;
+      rd = ldrec<T, SM>(rec + (d - base) * 4);
+    } while (d < dhi - 1 && rd.w <= xs);
+  }
+  // offset of the edge into its cell, from the two nearby pairs
   T a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
+  T w0 = rd.z;
   if (a < T(0) && d > dlo) {
     --d;
-    a += rec[(size_t)(d - base) * 4 + 2];
+    w0 = rec[(d - base) * 4 + 2];
+    a += w0;
   }
   const T sig = A4.z + A4.w;
   T b = a + sig;
@@ -614,19 +633,19 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
   // 1 / dImg), folded into each cell's overlap weight
   T wv = T(1);
   if (KIND == kB) {
-    if (P.scan == kFanED) wv = cweight_ed(src2[0], src2[1], pcx, pcy, P.s2r) / sig;
-    else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(src2[0], src2[1], pcx, pcy) * sig);
+    if (P.scan == kFanED) wv = cweight_ed(sx, sy, pcx, pcy, P.s2r) / sig;
+    else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(sx, sy, pcx, pcy) * sig);
     else wv = T(1) / P.dImg;
   }
-  // first kUnroll cells straight-line (cells past the pixel or the range get
-  // weight 0 on a clamped, valid cell), then the rare remainder
-  T ovj[kUnroll];
-  int dj[kUnroll];
+  // first U cells straight-line (cells past the pixel or the range get weight
+  // 0 on a clamped, valid cell), then the rare remainder
+  T ovj[U];
+  int oj[U];
 #pragma unroll
-  for (int j = 0; j < kUnroll; ++j) {
+  for (int j = 0; j < U; ++j) {
     const bool inside = d + j < dhi;
-    dj[j] = inside ? d + j : dhi - 1;
-    const T w = rec[(size_t)(dj[j] - base) * 4 + 2];
+    oj[j] = (inside ? d + j : dhi - 1) - base;
+    const T w = j == 0 ? w0 : rec[oj[j] * 4 + 2];
     T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
     ovj[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
     a -= w;
@@ -634,23 +653,23 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
   }
 #pragma unroll
   for (int qd = 0; qd < NQ; ++qd) {
-    T qq[kUnroll][QW];
+    T qq[U][QW];
 #pragma unroll
-    for (int j = 0; j < kUnroll; ++j) ldq<T, QW, SM>(qv + ((size_t)qd * qs + (dj[j] - base)) * QW, qq[j]);
+    for (int j = 0; j < U; ++j) ldq<T, QW, SM>(qv + (qd * qs + oj[j]) * QW, qq[j]);
 #pragma unroll
-    for (int j = 0; j < kUnroll; ++j)
+    for (int j = 0; j < U; ++j)
 #pragma unroll
       for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
   }
-  for (d += kUnroll; b > T(0) && d < dhi; ++d) {
-    const T w = rec[(size_t)(d - base) * 4 + 2];
+  for (d += U; b > T(0) && d < dhi; ++d) {
+    const T w = rec[(d - base) * 4 + 2];
     T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
     if (ov > T(0)) {
       if (KIND == kB) ov *= wv;
 #pragma unroll
       for (int qd = 0; qd < NQ; ++qd) {
         T qq[QW];
-        ldq<T, QW, SM>(qv + ((size_t)qd * qs + (d - base)) * QW, qq);
+        ldq<T, QW, SM>(qv + (qd * qs + (d - base)) * QW, qq);
 #pragma unroll
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ov, qq[i], blk[qd * QW + i]);
       }
@@ -662,14 +681,14 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
 
 // view v of pixel (r, c), everything read from the global tables; q planes of
 // view v start at qv with stride qs
-template <class T, int SB, int KIND>
+template <class T, int SB, int KIND, int U>
 __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int r, int c, const T* __restrict__ qv,
                                                 int qs, T pcx, T pcy, T (&blk)[SB]) {
   const bool xb = P.flags[v] & 1;
   const int k = xb ? c : P.H - 1 - r;
   const Quad<T> A4 = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r : c)) * 4);
-  pix_view<T, SB, KIND, false>(P, A4, k, P.inv + (size_t)v * 5, P.src + 2 * v, pcx, pcy,
-                               P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
+  pix_view<T, SB, KIND, U, false>(P, A4, k, load_seed(P.inv + (size_t)v * 5), P.src[2 * v], P.src[2 * v + 1], pcx,
+                                  pcy, P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
 }
 
 // Staged image gather. A CTA is a 32 x R pixel tile (R consumer warps, lane =
@@ -695,15 +714,16 @@ struct PixSlot {
   static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
 };
 
-template <class T, int SB, int KIND>
+template <class T, int SB, int KIND, int U>
 __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
   __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
-  __shared__ int s_ws[kSlots], s_fl[kSlots], s_l0[kSlots];
-  __shared__ float s_inv[kSlots][5];
+  // slot header, two 16-byte words: (window start or -1, flags, first line,
+  // seed a) and seed (b, c, d, e); the source position for the backprojector
+  __shared__ int4 s_hdr[kSlots][2];
   __shared__ T s_src[kSlots][2];
   __shared__ int s_bad;
   extern __shared__ __align__(16) unsigned char pix_smem[];
@@ -732,7 +752,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
     // one more dependent load, usually without correction steps.
     struct ViewIn {
       int fl;
-      float inv[5];
+      Seed sd;
       T sx, sy;
       Quad<T> A4[2];
     };
@@ -740,8 +760,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
       in.fl = 0;
       if (v >= V) return;
       in.fl = P.flags[v];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) in.inv[j] = P.inv[(size_t)v * 5 + j];
+      in.sd = load_seed(P.inv + (size_t)v * 5);
       in.sx = P.src[2 * v];
       in.sy = P.src[2 * v + 1];
       const bool xb = in.fl & 1;
@@ -763,7 +782,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
       for (int e = 0; e < 4; ++e) {
         const Quad<T>& A4 = in.A4[e & 1];
         xs[e] = add_rn(A4.x, mul_rn(A4.z, T((e & 2) ? kb : ka)));
-        d[e] = seed_cell(P.scan, (float)xs[e], in.inv, 0, D);
+        d[e] = seed_cell(P.scan, (float)xs[e], in.sd, 0, D);
         lo_b[e] = db2v[2 * d[e]];
         hi_b[e] = db2v[2 * d[e] + 2];
       }
@@ -801,11 +820,9 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
         const int nlj = __shfl_sync(0xffffffffu, nl, j);
         const bool staged = wsj >= 0 && !ld_volatile(s_bad);
         if (lane == j) {
-          s_ws[slot] = staged ? ws : -1;
-          s_fl[slot] = cur.fl;
-          s_l0[slot] = l0;
-#pragma unroll
-          for (int i = 0; i < 5; ++i) s_inv[slot][i] = cur.inv[i];
+          s_hdr[slot][0] = make_int4(staged ? ws : -1, cur.fl, l0, __float_as_int(cur.sd.a));
+          s_hdr[slot][1] = make_int4(__float_as_int(cur.sd.b), __float_as_int(cur.sd.c), __float_as_int(cur.sd.d),
+                                     __float_as_int(cur.sd.e));
           s_src[slot][0] = cur.sx;
           s_src[slot][1] = cur.sy;
         }
@@ -860,18 +877,23 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
       if (!ok) report_timeout(&s_bad);
     }
     if (active) {
-      const int ws = ok ? s_ws[slot] : -1;
-      if (ws >= 0) {
-        const bool xb = s_fl[slot] & 1;
-        const unsigned char* sl = slots + (size_t)slot * S::kBytes;
+      const int4 h0 = ok ? s_hdr[slot][0] : make_int4(-1, 0, 0, 0);
+      if (h0.x >= 0) {
+        const int4 h1 = s_hdr[slot][1];
+        const Seed sd{__int_as_float(h0.w), __int_as_float(h1.x), __int_as_float(h1.y), __int_as_float(h1.z),
+                      __int_as_float(h1.w)};
+        const bool xb = h0.y & 1;
+        const unsigned char* sl = slots + slot * S::kBytes;
         const T* sq = reinterpret_cast<const T*>(sl);
         const T* srec = reinterpret_cast<const T*>(sl + S::kQBytes);
         const T* slp = reinterpret_cast<const T*>(sl + S::kQBytes + S::kRecBytes);
-        const Quad<T> A4 = ldrec<T, true>(slp + (size_t)((xb ? r : c) - s_l0[slot]) * 4);
-        pix_view<T, SB, KIND, true>(P, A4, xb ? c : P.H - 1 - r, s_inv[slot], s_src[slot], pcx, pcy, srec, sq,
-                                    kWin, ws, ws, min(ws + kWin, D), blk);
+        const Quad<T> A4 = ldrec<T, true>(slp + ((xb ? r : c) - h0.z) * 4);
+        T sx = T(0), sy = T(0);
+        if (KIND == kB) { sx = s_src[slot][0]; sy = s_src[slot][1]; }
+        pix_view<T, SB, KIND, U, true>(P, A4, xb ? c : P.H - 1 - r, sd, sx, sy, pcx, pcy, srec, sq, kWin, h0.x,
+                                       h0.x, min(h0.x + kWin, D), blk);
       } else {
-        pix_view_global<T, SB, KIND>(P, v, r, c, qg + (size_t)v * NQ * Dp * QW, Dp, pcx, pcy, blk);
+        pix_view_global<T, SB, KIND, U>(P, v, r, c, qg + (size_t)v * NQ * Dp * QW, Dp, pcx, pcy, blk);
       }
     }
     __syncwarp();
@@ -900,7 +922,7 @@ __device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int 
   kahan_init_smem<T, 1>(acc);
   T blk[1] = {T(0)};
   for (int v = 0; v < P.V; ++v) {
-    pix_view_global<T, 1, KIND>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
+    pix_view_global<T, 1, KIND, 3>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
     if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk);
   }
   kahan_fold_smem<T, 1>(acc, blk);
@@ -1033,6 +1055,9 @@ struct ctgb_plan {
   // per CTA of the gather kernel (8 or 4)
   int sb_cap[5] = {0, 0, 0, 0, 0};
   int warps[5] = {8, 8, 8, 8, 8};
+  // straight-line steps of the gather loop (3 or 2; 2 is built for fp32 with
+  // 4 or more slices per thread, other widths always use 3)
+  int unroll[5] = {3, 3, 3, 3, 3};
   void* dev = nullptr;  // one allocation holding all tables
   ctgb::DevPlan<float> pf{};
   ctgb::DevPlan<double> pd{};
@@ -1142,6 +1167,10 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
 }
 
+// two straight-line steps are instantiated for the widths that carry batches
+template <class T, int SB>
+constexpr bool kTwoStep = sizeof(T) == 4 && SB >= 4;
+
 template <class T, int SB>
 static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* in, void* out, int batch,
                   void* ws, cudaStream_t st) {
@@ -1168,10 +1197,15 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     const int wpc = p->warps[op];
     dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
     const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
-    if (op == CTGB_OP_PROJECTION)
-      k_det_gather<T, SB, kA><<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
-    else
-      k_det_gather<T, SB, kBt><<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
+    const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
+    auto launch = [&](auto kern) { kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch); };
+    if (op == CTGB_OP_PROJECTION) {
+      if (two) launch(k_det_gather<T, SB, kA, kTwoStep<T, SB> ? 2 : 3>);
+      else launch(k_det_gather<T, SB, kA, 3>);
+    } else {
+      if (two) launch(k_det_gather<T, SB, kBt, kTwoStep<T, SB> ? 2 : 3>);
+      else launch(k_det_gather<T, SB, kBt, 3>);
+    }
   } else {
     T* qb = static_cast<T*>(ws);
     if (op == CTGB_OP_FBP) {
@@ -1205,10 +1239,15 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
       kern<<<grid, nt, smem, st>>>(P, qb, y, batch, mul, div);
       return CTGB_OK;
     };
+    constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
+    const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
     int rc;
-    if (op == CTGB_OP_PROJECTION_T) rc = launch(k_pix_gather<T, SB, kAt>, T(1), T(1));
-    else if (op == CTGB_OP_BACKPROJECTION) rc = launch(k_pix_gather<T, SB, kB>, T(1), T(1));
-    else rc = launch(k_pix_gather<T, SB, kB>, P.dAng, T(2));
+    if (op == CTGB_OP_PROJECTION_T)
+      rc = two ? launch(k_pix_gather<T, SB, kAt, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kAt, 3>, T(1), T(1));
+    else if (op == CTGB_OP_BACKPROJECTION)
+      rc = two ? launch(k_pix_gather<T, SB, kB, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kB, 3>, T(1), T(1));
+    else
+      rc = two ? launch(k_pix_gather<T, SB, kB, U2>, P.dAng, T(2)) : launch(k_pix_gather<T, SB, kB, 3>, P.dAng, T(2));
     if (rc != CTGB_OK) return rc;
   }
   cudaError_t e = cudaGetLastError();
@@ -1304,7 +1343,7 @@ __global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<float>* __
     const DevPlan<float> P = plans[tk.slice];
     const int v = tk.a * (blockDim.x >> 5) + warp, d = tk.b * 32 + lane;
     if (v < P.V && d < P.D)
-      det_gather_cell<float, 1, KIND>(P, v, d, 0, io.in[tk.slice],
+      det_gather_cell<float, 1, KIND, 3>(P, v, d, 0, io.in[tk.slice],
                                       reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice], 1);
   }
 }
@@ -1643,6 +1682,14 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
     return ctgb::fail(CTGB_ERR_INVALID, "warps_per_cta must be 0 (default), 4 or 8");
   plan->sb_cap[op] = slices_per_thread;
   plan->warps[op] = warps_per_cta == 0 ? 8 : warps_per_cta;
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps) {
+  if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
+  if (op < 0 || op > 4) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
+  if (!(steps == 0 || steps == 2 || steps == 3)) return ctgb::fail(CTGB_ERR_INVALID, "steps must be 0 (default), 2 or 3");
+  plan->unroll[op] = steps == 0 ? 3 : steps;
   return CTGB_OK;
 }
 

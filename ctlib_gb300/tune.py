@@ -1,11 +1,14 @@
 """Autotuner for the operators' launch schedules.
 
-A schedule is (slices carried per thread, warps per CTA) for one operator on one
-plan (`ctgb_plan_set_schedule`). Carrying more slices per thread amortises the
-per-(view, line) geometry over more fused multiply-adds but costs registers
-and therefore resident warps; fewer warps per CTA changes how views (detector
-gather) or image rows (image gather) are grouped for L1 reuse. The best choice
-depends on the geometry, the batch and the GPU, so it is measured: every
+A schedule is (slices carried per thread, warps per CTA, straight-line steps)
+for one operator on one plan (`ctgb_plan_set_schedule`, `ctgb_plan_set_unroll`).
+Carrying more slices per thread amortises the per-(view, line) geometry over
+more fused multiply-adds but costs registers and therefore resident warps;
+fewer warps per CTA changes how views (detector gather) or image rows (image
+gather) are grouped; two straight-line steps instead of three skip the third
+pixel (cell) that most cells (pixels) do not reach, at the price of a
+divergent remainder loop where some do. The best choice depends on the
+geometry, the batch and the GPU, so it is measured: every
 candidate is timed with CUDA events on the caller's device and the fastest is
 kept, in memory and in a JSON cache on disk
 (``$CTLIB_GB300_TUNE_CACHE``, default ``~/.cache/ctlib_gb300/tune.json``).
@@ -24,8 +27,8 @@ import torch
 
 from . import _native as N
 
-CANDIDATES_F32 = ((16, 8), (16, 4), (8, 8), (8, 4), (4, 8))
-CANDIDATES_F64 = ((4, 8), (4, 4), (2, 8))
+CANDIDATES_F32 = ((16, 8, 3), (16, 8, 2), (16, 4, 3), (16, 4, 2), (8, 8, 3), (8, 8, 2), (8, 4, 2), (4, 8, 2))
+CANDIDATES_F64 = ((4, 8, 3), (4, 4, 3), (2, 8, 3))
 
 _lock = threading.Lock()
 _cache = None
@@ -64,13 +67,14 @@ def _key(plan, op: int, batch: int) -> str:
     return f"{name}|{plan.dtype}|{op}|{batch}|{','.join(repr(v) for v in plan.values)}"
 
 
-def _set(plan, op: int, sb: int, warps: int):
+def _set(plan, op: int, sb: int, warps: int, unroll: int = 0):
     """Set the plan's schedule for `op` unless it is already the current one
     (one plan serves every batch size, each with its own tuned schedule)."""
     cur = plan.__dict__.setdefault("_current", {})
-    if cur.get(op) != (sb, warps):
+    if cur.get(op) != (sb, warps, unroll):
         N.check(N.lib().ctgb_plan_set_schedule(plan.handle, op, sb, warps), "schedule")
-        cur[op] = (sb, warps)
+        N.check(N.lib().ctgb_plan_set_unroll(plan.handle, op, unroll), "schedule")
+        cur[op] = (sb, warps, unroll)
 
 
 def apply_cached(plan, op: int, batch: int) -> bool:
@@ -82,9 +86,11 @@ def apply_cached(plan, op: int, batch: int) -> bool:
         if hit is None and os.environ.get("CTLIB_GB300_AUTOTUNE") == "1":
             tune(plan, op, batch)
             hit = memo[(op, batch)]
-        memo[(op, batch)] = None if hit is None else (int(hit[0]), int(hit[1]))
+        if hit is not None and len(hit) == 3:  # older cache entry: (sb, warps, ms)
+            hit = [hit[0], hit[1], 0, hit[2]]
+        memo[(op, batch)] = None if hit is None else (int(hit[0]), int(hit[1]), int(hit[2]))
     sched = memo[(op, batch)]
-    _set(plan, op, *(sched if sched is not None else (0, 0)))
+    _set(plan, op, *(sched if sched is not None else (0, 0, 0)))
     return sched is not None
 
 
@@ -105,8 +111,8 @@ def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
     stream = torch.cuda.current_stream(x.device)
     results = []
     with torch.cuda.device(x.device):
-        for sb, warps in candidates:
-            _set(plan, op, sb, warps)
+        for sb, warps, unroll in candidates:
+            _set(plan, op, sb, warps, unroll)
             plan.run(op, x, out)  # warm-up (and workspace size for this schedule)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -114,13 +120,14 @@ def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
                 plan.run(op, x, out)
             b.record(stream)
             torch.cuda.synchronize(x.device)
-            results.append((a.elapsed_time(b) / reps, sb, warps))
+            results.append((a.elapsed_time(b) / reps, sb, warps, unroll))
     results.sort()
-    best_ms, sb, warps = results[0]
-    _set(plan, op, sb, warps)
+    best_ms, sb, warps, unroll = results[0]
+    _set(plan, op, sb, warps, unroll)
     with _lock:
-        _load()[_key(plan, op, batch)] = [sb, warps, best_ms]
+        _load()[_key(plan, op, batch)] = [sb, warps, unroll, best_ms]
         _save()
-    plan.__dict__.setdefault("_tuned", {})[(op, batch)] = (sb, warps)
-    return {"slices_per_thread": sb, "warps_per_cta": warps, "ms": best_ms,
-            "candidates": [{"slices_per_thread": s, "warps_per_cta": w, "ms": m} for m, s, w in results]}
+    plan.__dict__.setdefault("_tuned", {})[(op, batch)] = (sb, warps, unroll)
+    return {"slices_per_thread": sb, "warps_per_cta": warps, "unroll": unroll, "ms": best_ms,
+            "candidates": [{"slices_per_thread": s, "warps_per_cta": w, "unroll": u, "ms": m}
+                           for m, s, w, u in results]}

@@ -66,6 +66,15 @@ int ctgb_plan_info(const ctgb_plan* plan, int* views, int* dets, int* width, int
  * (slice, view, 256-bin block), src/fan_ed_kernel.cu:1179-1185). */
 int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int warps_per_cta);
 
+/* Straight-line steps of one operator's gather loop (2 or 3; 0 = default 3):
+ * the overlapped pixels per detector cell (projection, backprojection_t) or
+ * cells per pixel (projection_t, backprojection, fbp) evaluated without a
+ * branch before a remainder loop takes any further ones. 2 pays when few cells
+ * (pixels) span three pixels (cells); fp32 with 4 or more slices per thread
+ * only, other widths always use 3. Results do not depend on it. No counterpart
+ * in the reference (its merge walk has no fixed step count). */
+int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps);
+
 /* Scratch bytes `op` needs for `batch` slices (0 is a valid answer). */
 size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch);
 

@@ -176,14 +176,25 @@ def test_image_gather_staged_and_global_views(ct, oracle_mod, scan, batch):
     reads the global tables otherwise. These geometries mix both kinds of views
     within one launch; the result must match the FP64 oracle either way, and no
     bounded wait of the copy pipeline may have run out."""
-    from ctlib_gb300 import _native
+    from ctlib_gb300 import _native, ops
     O = oracle_mod
     opts = _fine_geom(scan)
     rng = np.random.default_rng(100 + 10 * scan + batch)
     sino = rng.standard_normal((batch, 1, 60, int(opts[1]))).astype(np.float32)
     before = _native.wait_timeouts(0)
+    o = torch.tensor(opts, dtype=torch.float32)
+    plan = ops.get_plan(o, torch.float32, torch.device("cuda", 0))
     for op in ("projection_t", "backprojection", "fbp"):
         got = _run(ct, op, sino, opts)
         want = O.run(op, sino, opts, O.MODE_F64_ON_F32)
         assert O.rel_l2(got, want) <= 1e-5, (op, O.rel_l2(got, want))
+        # two straight-line cells per pixel, the rest in the remainder loop:
+        # the same sums in the same order
+        code = getattr(_native, "OP_" + op.upper())
+        plan.__dict__.setdefault("_tuned", {})[(code, batch)] = (0, 8, 2)
+        try:
+            two = _run(ct, op, sino, opts)
+        finally:
+            del plan._tuned[(code, batch)]
+        assert np.array_equal(two, got), op
     assert _native.wait_timeouts(0) == before

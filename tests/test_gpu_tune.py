@@ -1,5 +1,6 @@
-"""Autotuned schedules change only the launch shape: outputs must be identical
-to the default schedule's, bit for bit, and the choice must be cached."""
+"""Autotuned schedules (slices per thread, warps per CTA, straight-line steps)
+change only the launch shape: outputs must be identical to the default
+schedule's, bit for bit, and the choice must be cached."""
 
 import math
 import os
@@ -26,6 +27,8 @@ def test_tune_keeps_results_and_caches(tmp_path, monkeypatch):
     plan = ops.get_plan(o, torch.float32, img.device)
     ref_a = ops.projection(img, o)
     ref_at = ops.projection_t(ref_a, o)
+    ref_bt = ops.backprojection_t(img, o)
+    ref_b = ops.backprojection(ref_a, o)
     for op in (N.OP_PROJECTION, N.OP_PROJECTION_T):
         r = tune.tune(plan, op, img.shape[0], reps=1)
         assert len(r["candidates"]) >= 3
@@ -34,12 +37,14 @@ def test_tune_keeps_results_and_caches(tmp_path, monkeypatch):
     tune.tune(plan, N.OP_PROJECTION, 1, reps=1)
     ops.projection(img, o)
     assert plan._current[N.OP_PROJECTION] == plan._tuned[(N.OP_PROJECTION, img.shape[0])]
-    for sb, warps in tune.CANDIDATES_F32:
-        for op in (N.OP_PROJECTION, N.OP_PROJECTION_T):
-            plan._tuned[(op, img.shape[0])] = (sb, warps)  # force this schedule for the batch
+    for sched in tune.CANDIDATES_F32:
+        for op in (N.OP_PROJECTION, N.OP_PROJECTION_T, N.OP_BACKPROJECTION, N.OP_BACKPROJECTION_T):
+            plan._tuned[(op, img.shape[0])] = sched  # force this schedule for the batch
         a = ops.projection(img, o)
         at = ops.projection_t(a, o)
-        assert plan._current[N.OP_PROJECTION] == (sb, warps)
-        assert torch.equal(a, ref_a), (sb, warps)
-        assert torch.equal(at, ref_at), (sb, warps)
+        assert plan._current[N.OP_PROJECTION] == sched
+        assert torch.equal(a, ref_a), sched
+        assert torch.equal(at, ref_at), sched
+        assert torch.equal(ops.backprojection_t(img, o), ref_bt), sched
+        assert torch.equal(ops.backprojection(ref_a, o), ref_b), sched
     ops.clear_plans()
