@@ -305,16 +305,19 @@ def run_ours(args):
 
     # -- roofline of the dominant kernel -------------------------------------
     ta, tat = statistics.mean(t_a), statistics.mean(t_at)
-    dom = "det_gather (projection)" if ta >= tat else "pix_gather (projection_t)"
-    dom_ms = max(ta, tat)
+    ka, kat = _kernel_times(plan, args.steps, flush, stream, lambda: ctlib.projection(img, opts),
+                            lambda s: ctlib.projection_t(s, opts))
+    dom = "k_det_gather (projection)" if ka >= kat else "k_pix_gather (projection_t)"
+    dom_ms = max(ka, kat)
     # algorithmic bytes of one launch: read input + write output once
     alg_bytes = (B * H * W + B * V * D) * 4
     hbm_peak = _measured("hbm_gbs", 6790.7)
     achieved_gbs = alg_bytes / (dom_ms / 1e3) / 1e9
     peak = _fp32_peak(dev) if rank == 0 else None
     roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak[0], "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(), "peak_source": hbm_peak[1],
-            "kernel": dom, "kernel_ms": dom_ms, "algorithmic_bytes": alg_bytes}
+            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(dom.split()[0]), "peak_source": hbm_peak[1],
+            "kernel": dom, "kernel_ms": dom_ms, "algorithmic_bytes": alg_bytes,
+            "timing": "CUDA events recorded by the library right around the kernel, mean of the timed steps"}
     roof_fp32 = None
     if peak:
         # survey model: 8 FP32 lane-ops per ray-update at the measured FFMA rate
@@ -339,6 +342,7 @@ def run_ours(args):
                           "note": "one projection + projection_t call per slice"},
                 "batched_over_plain": value / ws / plain_value,
                 "ms_projection": ta, "ms_projection_t": tat,
+                "kernel_ms": {"k_det_gather": ka, "k_pix_gather": kat},
                 "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_mean,
                         "h2d_bytes_per_step": int(img_h.numel() * 4),
                         "d2h_bytes_per_step": int(img_h.numel() * 4 + 4),
@@ -418,6 +422,39 @@ def run_ragged(args):
     return 0
 
 
+def _kernel_times(plan, steps, flush, stream, run_a, run_at):
+    """Mean durations (ms) of the gather kernel of projection and of
+    projection_t alone: the library records caller events right around each
+    gather launch (ctgb_plan_set_kernel_events), on the launching stream."""
+    import torch
+    from ctlib_gb300 import _native as N
+    evs = []
+    for _ in range(steps):
+        pair = []
+        for _ in range(2):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)  # creates the CUDA events behind the handles
+            b.record(stream)
+            pair.append((a, b))
+        evs.append(pair)
+    torch.cuda.synchronize()
+    lib = N.lib()
+    try:
+        for i in range(steps):
+            flush.fill_(float(i))
+            (a0, b0), (a1, b1) = evs[i]
+            N.check(lib.ctgb_plan_set_kernel_events(plan.handle, a0.cuda_event, b0.cuda_event), "kernel events")
+            s = run_a()
+            N.check(lib.ctgb_plan_set_kernel_events(plan.handle, a1.cuda_event, b1.cuda_event), "kernel events")
+            run_at(s)
+    finally:
+        lib.ctgb_plan_set_kernel_events(plan.handle, None, None)
+    torch.cuda.synchronize()
+    ka = statistics.mean(evs[i][0][0].elapsed_time(evs[i][0][1]) for i in range(steps))
+    kt = statistics.mean(evs[i][1][0].elapsed_time(evs[i][1][1]) for i in range(steps))
+    return ka, kt
+
+
 def _measured(key, fallback):
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -427,15 +464,17 @@ def _measured(key, fallback):
         return fallback, "fallback"
 
 
-def _ncu_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary, if one exists (profiles/*.json written from an ncu capture)."""
+def _ncu_traffic(kernel: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
+    summary (profiles/dram_traffic.json, written from an ncu capture of the
+    same workload and schedule), or None."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get("bytes_per_launch")
+            entry = json.load(f).get("kernels", {}).get(kernel)
     except (OSError, ValueError):
         return None
+    return None if entry is None else entry.get("bytes_per_launch")
 
 
 def main():

@@ -76,6 +76,8 @@ def _declare(l):
     l.ctgb_plan_set_schedule.restype = c_int
     l.ctgb_plan_set_unroll.argtypes = [vp, c_int, c_int]
     l.ctgb_plan_set_unroll.restype = c_int
+    l.ctgb_plan_set_kernel_events.argtypes = [vp, vp, vp]
+    l.ctgb_plan_set_kernel_events.restype = c_int
     l.ctgb_workspace_size.argtypes = [vp, c_int, c_int]
     l.ctgb_workspace_size.restype = c_size
     for name in ("ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
@@ -135,6 +137,7 @@ def check(rc: int, what: str):
 
 
 EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_plan_set_schedule", "ctgb_plan_set_unroll",
+            "ctgb_plan_set_kernel_events",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
             "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",

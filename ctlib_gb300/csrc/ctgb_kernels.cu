@@ -1058,6 +1058,9 @@ struct ctgb_plan {
   // straight-line steps of the gather loop (3 or 2; 2 is built for fp32 with
   // 4 or more slices per thread, other widths always use 3)
   int unroll[5] = {3, 3, 3, 3, 3};
+  // optional events recorded right before and after each gather kernel on the
+  // launch stream (ctgb_plan_set_kernel_events), to time that kernel alone
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   void* dev = nullptr;  // one allocation holding all tables
   ctgb::DevPlan<float> pf{};
   ctgb::DevPlan<double> pd{};
@@ -1198,7 +1201,11 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
     const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
     const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
-    auto launch = [&](auto kern) { kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch); };
+    auto launch = [&](auto kern) {
+      if (p->ev_start) cudaEventRecord(p->ev_start, st);
+      kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
+      if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
+    };
     if (op == CTGB_OP_PROJECTION) {
       if (two) launch(k_det_gather<T, SB, kA, kTwoStep<T, SB> ? 2 : 3>);
       else launch(k_det_gather<T, SB, kA, 3>);
@@ -1236,7 +1243,9 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     auto launch = [&](auto kern, T mul, T div) -> int {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
+      if (p->ev_start) cudaEventRecord(p->ev_start, st);
       kern<<<grid, nt, smem, st>>>(P, qb, y, batch, mul, div);
+      if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
       return CTGB_OK;
     };
     constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
@@ -1682,6 +1691,15 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
     return ctgb::fail(CTGB_ERR_INVALID, "warps_per_cta must be 0 (default), 4 or 8");
   plan->sb_cap[op] = slices_per_thread;
   plan->warps[op] = warps_per_cta == 0 ? 8 : warps_per_cta;
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_kernel_events(ctgb_plan* plan, void* start_event, void* stop_event) {
+  if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
+  if ((start_event == nullptr) != (stop_event == nullptr))
+    return ctgb::fail(CTGB_ERR_INVALID, "give both events or neither");
+  plan->ev_start = static_cast<cudaEvent_t>(start_event);
+  plan->ev_stop = static_cast<cudaEvent_t>(stop_event);
   return CTGB_OK;
 }
 

@@ -75,6 +75,14 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
  * in the reference (its merge walk has no fixed step count). */
 int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps);
 
+/* Measurement hook: when both are non-null, every later operator call on this
+ * plan records `start_event` right before its gather kernel and `stop_event`
+ * right after it, on the call's stream (cudaEvent_t handles created with
+ * timing enabled), so cudaEventElapsedTime gives that kernel's own duration;
+ * NULL, NULL turns it off. Not thread-safe against concurrent calls on the same
+ * plan. No counterpart in the reference. */
+int ctgb_plan_set_kernel_events(ctgb_plan* plan, void* start_event, void* stop_event);
+
 /* Scratch bytes `op` needs for `batch` slices (0 is a valid answer). */
 size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch);
 
