@@ -98,10 +98,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _cpu_baseline(w, seconds_target: float = 15.0) -> dict:
-    """The CPU oracle (fp32, reference promotions) on a bounded sample of the
-    workload: one slice, a contiguous subset of the views, A then A^T, all
-    host threads. Returned in ray-updates/s."""
+def _cpu_step(w, step_seconds: float):
+    """One step of the CPU arm: the OpenMP oracle port (fp32, reference type
+    promotions) running projection then projection_t on a bounded sample of the
+    workload, one slice and a contiguous subset of its views sized to about
+    `step_seconds`, on all host threads. Returns (step, ray-updates per step,
+    sample description, threads)."""
     import oracle
     from ctlib_gb300.workloads import ellipse_phantom
     s = w.slices[0]
@@ -109,33 +111,45 @@ def _cpu_baseline(w, seconds_target: float = 15.0) -> dict:
     V, D, W, H = (int(o[i]) for i in range(4))
     threads = oracle.max_threads()
     img = ellipse_phantom(H, W, o[4], s.seed)[None, None]
+    sub = list(o)
+
+    def step():
+        sino = oracle.run("projection", img, sub, oracle.MODE_F32, threads)
+        oracle.run("projection_t", sino, sub, oracle.MODE_F32, threads)
+
     nv = 16
     while True:
-        sub = list(o)
         sub[0] = float(nv)
         t0 = time.perf_counter()
-        sino = oracle.run("projection", img, sub, oracle.MODE_F32, threads)
-        oracle.run("projection_t", sino, sub, oracle.MODE_F32, threads)
+        step()
         dt = time.perf_counter() - t0
-        if dt > seconds_target / 4 or nv >= V:
+        if dt > step_seconds / 2 or nv >= V:
             break
-        nv = min(V, int(nv * max(2.0, seconds_target / 4 / max(dt, 1e-3))))
-    reps = max(1, int(seconds_target / max(dt, 1e-3)))
-    reps = min(reps, 8)
+        nv = min(V, int(nv * max(2.0, step_seconds / max(dt, 1e-3))))
+    ru = 2 * nv * D * max(W, H)
+    return step, ru, f"1 slice of {w.name}, views 0..{nv - 1} of {V}, projection + projection_t", threads
+
+
+def _cpu_baseline(w, seconds_target: float = 15.0) -> dict:
+    """The CPU arm timed over about `seconds_target` seconds of repeated steps,
+    in ray-updates/s."""
+    step, ru, sample, threads = _cpu_step(w, 1.0)
+    t0 = time.perf_counter()
+    step()
+    one = time.perf_counter() - t0
+    reps = max(1, int(round(seconds_target / max(one, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(reps):
-        sino = oracle.run("projection", img, sub, oracle.MODE_F32, threads)
-        oracle.run("projection_t", sino, sub, oracle.MODE_F32, threads)
+        step()
     dt = (time.perf_counter() - t0) / reps
-    ru = 2 * nv * D * max(W, H)
     return {"value": ru / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"1 slice of {w.name}, views 0..{nv - 1} of {V}, projection + projection_t, "
-                      f"{reps} rep(s), {dt:.2f} s each"}
+            "sample": f"{sample}, {reps} rep(s) of {dt:.2f} s"}
 
 
 def run_reference(args):
     """Reference arm: the reference has no CPU path; its distance-driven loops
-    run as the OpenMP oracle port on the host cores."""
+    run as the OpenMP oracle port on the host cores (all threads), each step a
+    bounded sample of the workload (about 2 s), W warm-up and K timed steps."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
@@ -143,13 +157,25 @@ def run_reference(args):
     from oracle import build as obuild
     obuild.build_oracle()
     w = WORKLOADS[args.workload]()
-    cb = _cpu_baseline(w, seconds_target=max(5.0, 20.0 / max(1, args.steps)))
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic ellipse phantoms",
-            "config": {"workload": w.name, "global_batch": len(w.slices), "cpu_sample": cb["sample"]},
+    step, ru, sample, threads = _cpu_step(w, 2.0)
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = ru / (ms / 1e3)
+    cb = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"{sample}, per step"}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic ellipse phantoms (seeded)",
+            "config": {"workload": w.name, "global_batch": len(w.slices), "cpu_sample": sample,
+                       "ray_updates_per_step": ru},
             "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
     return 0
