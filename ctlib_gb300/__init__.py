@@ -8,8 +8,8 @@ The operators run hand-written sm_103a CUDA kernels (``csrc/``) behind the C ABI
 declared in ``include/ctgb.h``; there is no CPU path.
 """
 
-from .ops import (backprojection, backprojection_t, clear_plans, fbp, get_plan, projection,  # noqa: F401
-                  projection_t)
+from .ops import (backprojection, backprojection_sv, backprojection_t, clear_plans, fbp, get_plan,  # noqa: F401
+                  projection, projection_t)
 
-__all__ = ["projection", "projection_t", "backprojection", "backprojection_t", "fbp", "get_plan",
-           "clear_plans"]
+__all__ = ["projection", "projection_t", "backprojection", "backprojection_t", "fbp", "backprojection_sv",
+           "get_plan", "clear_plans"]

@@ -25,6 +25,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 OK, ERR_INVALID, ERR_CUDA, ERR_WORKSPACE = 0, 1, 2, 3
 OP_PROJECTION, OP_PROJECTION_T, OP_BACKPROJECTION, OP_BACKPROJECTION_T, OP_FBP = 0, 1, 2, 3, 4
+OP_BACKPROJECTION_SV = 5
 
 _lock = threading.Lock()
 _lib = None
@@ -81,7 +82,7 @@ def _declare(l):
     l.ctgb_workspace_size.argtypes = [vp, c_int, c_int]
     l.ctgb_workspace_size.restype = c_size
     for name in ("ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
-                 "ctgb_fbp"):
+                 "ctgb_fbp", "ctgb_backprojection_sv"):
         f = getattr(l, name)
         f.argtypes = [vp, vp, vp, c_int, vp, c_size, vp]
         f.restype = c_int
@@ -140,7 +141,7 @@ EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_pla
             "ctgb_plan_set_kernel_events",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
-            "ctgb_fbp", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
+            "ctgb_fbp", "ctgb_backprojection_sv", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
             "ctgb_ragged_destroy", "ctgb_ragged_workspace_size", "ctgb_ragged_run", "ctgb_last_error",
             "ctgb_version", "ctgb_geometry_query", "ctgb_wait_timeouts")
 

@@ -714,7 +714,9 @@ struct PixSlot {
   static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
 };
 
-template <class T, int SB, int KIND, int U>
+// SV: single-view backprojection (src/fan_ed_kernel.cu:946-1161): each view's
+// sum goes to its own image, img[slice][view][row][col], with no sum over views.
+template <class T, int SB, int KIND, int U, bool SV = false>
 __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
@@ -876,6 +878,10 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
       ok = mbar_wait(&s_full[slot], (v / kSlots) & 1);
       if (!ok) report_timeout(&s_bad);
     }
+    if (SV) {
+#pragma unroll
+      for (int s = 0; s < SB; ++s) blk[s] = T(0);
+    }
     if (active) {
       const int4 h0 = ok ? s_hdr[slot][0] : make_int4(-1, 0, 0, 0);
       if (h0.x >= 0) {
@@ -898,8 +904,19 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&s_empty[slot]);
-    if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
+    if (SV) {
+      if (active) {
+#pragma unroll
+        for (int s = 0; s < SB; ++s) {
+          const int bb = g * SB + s;
+          if (bb < B) img[(((size_t)bb * V + v) * P.H + r) * P.W + c] = blk[s];
+        }
+      }
+    } else if ((v % kFoldEvery) == kFoldEvery - 1) {
+      kahan_fold_smem<T, SB>(acc, blk);
+    }
   }
+  if (SV) return;
   kahan_fold_smem<T, SB>(acc, blk);
   if (!active) return;
 #pragma unroll
@@ -1053,11 +1070,11 @@ struct ctgb_plan {
   int dtype = 0;
   // per-operator schedule: cap on slices per thread (0 = default) and warps
   // per CTA of the gather kernel (8 or 4)
-  int sb_cap[5] = {0, 0, 0, 0, 0};
-  int warps[5] = {8, 8, 8, 8, 8};
+  int sb_cap[6] = {0, 0, 0, 0, 0, 0};
+  int warps[6] = {8, 8, 8, 8, 8, 8};
   // straight-line steps of the gather loop (3 or 2; 2 is built for fp32 with
   // 4 or more slices per thread, other widths always use 3)
-  int unroll[5] = {3, 3, 3, 3, 3};
+  int unroll[6] = {3, 3, 3, 3, 3, 3};
   // optional events recorded right before and after each gather kernel on the
   // launch stream (ctgb_plan_set_kernel_events), to time that kernel alone
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
@@ -1251,7 +1268,10 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
     const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
     int rc;
-    if (op == CTGB_OP_PROJECTION_T)
+    if (op == CTGB_OP_BACKPROJECTION_SV)
+      rc = two ? launch(k_pix_gather<T, SB, kB, U2, true>, T(1), T(1))
+               : launch(k_pix_gather<T, SB, kB, 3, true>, T(1), T(1));
+    else if (op == CTGB_OP_PROJECTION_T)
       rc = two ? launch(k_pix_gather<T, SB, kAt, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kAt, 3>, T(1), T(1));
     else if (op == CTGB_OP_BACKPROJECTION)
       rc = two ? launch(k_pix_gather<T, SB, kB, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kB, 3>, T(1), T(1));
@@ -1268,6 +1288,8 @@ static int dispatch(const ctgb_plan* p, int op, const void* in, void* out, int b
                     void* stream) {
   if (!p) return fail(CTGB_ERR_INVALID, "null plan");
   if (batch < 0) return fail(CTGB_ERR_INVALID, "negative batch");
+  if (op == CTGB_OP_BACKPROJECTION_SV && p->geom.scan != kFanED)
+    return fail(CTGB_ERR_INVALID, "backprojection_sv is defined for equal-distance fan beams (scan_type 0) only");
   if (batch == 0) return CTGB_OK;
   if (!in || !out) return fail(CTGB_ERR_INVALID, "null input or output pointer");
   const size_t need = workspace_bytes(p, op, batch);
@@ -1683,7 +1705,7 @@ int ctgb_plan_info(const ctgb_plan* p, int* views, int* dets, int* width, int* h
 
 int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int warps_per_cta) {
   if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
-  if (op < 0 || op > 4) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
+  if (op < 0 || op > 5) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
   if (!(slices_per_thread == 0 || slices_per_thread == 1 || slices_per_thread == 2 || slices_per_thread == 4 ||
         slices_per_thread == 8 || slices_per_thread == 16))
     return ctgb::fail(CTGB_ERR_INVALID, "slices_per_thread must be 0 (default), 1, 2, 4, 8 or 16");
@@ -1705,14 +1727,14 @@ int ctgb_plan_set_kernel_events(ctgb_plan* plan, void* start_event, void* stop_e
 
 int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps) {
   if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
-  if (op < 0 || op > 4) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
+  if (op < 0 || op > 5) return ctgb::fail(CTGB_ERR_INVALID, "unknown operator");
   if (!(steps == 0 || steps == 2 || steps == 3)) return ctgb::fail(CTGB_ERR_INVALID, "steps must be 0 (default), 2 or 3");
   plan->unroll[op] = steps == 0 ? 3 : steps;
   return CTGB_OK;
 }
 
 size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch) {
-  if (!plan || batch <= 0 || op < 0 || op > 4) return 0;
+  if (!plan || batch <= 0 || op < 0 || op > 5) return 0;
   return ctgb::workspace_bytes(plan, op, batch);
 }
 
@@ -1734,6 +1756,10 @@ int ctgb_backprojection_t(const ctgb_plan* p, const void* image, void* sino, int
 }
 int ctgb_fbp(const ctgb_plan* p, const void* sino, void* image, int batch, void* ws, size_t wsb, void* stream) {
   return ctgb::dispatch(p, CTGB_OP_FBP, sino, image, batch, ws, wsb, stream);
+}
+int ctgb_backprojection_sv(const ctgb_plan* p, const void* sino, void* images, int batch, void* ws, size_t wsb,
+                           void* stream) {
+  return ctgb::dispatch(p, CTGB_OP_BACKPROJECTION_SV, sino, images, batch, ws, wsb, stream);
 }
 
 int ctgb_projection_noalloc(const ctgb_plan* p, const void* image, void* sino, int batch, void* stream) {

@@ -1,8 +1,9 @@
 """Drop-in replacements for the functions of CTLIB's ``ctlib`` module.
 
-``projection``, ``projection_t``, ``backprojection``, ``backprojection_t`` and
-``fbp`` take and return the same tensors as the reference (src/ctlib.cpp:15-99):
-images ``B x 1 x H x W``, sinograms ``B x 1 x V x D``, contiguous CUDA tensors
+``projection``, ``projection_t``, ``backprojection``, ``backprojection_t``,
+``fbp`` and ``backprojection_sv`` take and return the same tensors as the
+reference (src/ctlib.cpp:15-99): images ``B x 1 x H x W``, sinograms
+``B x 1 x V x D``, per-view images ``B x V x H x W``, contiguous CUDA tensors
 in float32 or float64, and the reference's options vector. Each call returns a
 fresh tensor on the input's device and launches on the current CUDA stream.
 
@@ -75,7 +76,8 @@ class Plan:
 
 
 _NAMES = {N.OP_PROJECTION: "projection", N.OP_PROJECTION_T: "projection_t",
-          N.OP_BACKPROJECTION: "backprojection", N.OP_BACKPROJECTION_T: "backprojection_t", N.OP_FBP: "fbp"}
+          N.OP_BACKPROJECTION: "backprojection", N.OP_BACKPROJECTION_T: "backprojection_t", N.OP_FBP: "fbp",
+          N.OP_BACKPROJECTION_SV: "backprojection_sv"}
 
 
 class _FnTable(dict):
@@ -83,7 +85,7 @@ class _FnTable(dict):
         l = N.lib()
         fn = {N.OP_PROJECTION: l.ctgb_projection, N.OP_PROJECTION_T: l.ctgb_projection_t,
               N.OP_BACKPROJECTION: l.ctgb_backprojection, N.OP_BACKPROJECTION_T: l.ctgb_backprojection_t,
-              N.OP_FBP: l.ctgb_fbp}[op]
+              N.OP_FBP: l.ctgb_fbp, N.OP_BACKPROJECTION_SV: l.ctgb_backprojection_sv}[op]
         self[op] = fn
         return fn
 
@@ -167,6 +169,12 @@ def _apply(op: int, x: torch.Tensor, options, name: str) -> torch.Tensor:
         if tuple(x.shape[2:]) != img_shape:
             raise ValueError(f"{name}: image is {tuple(x.shape[2:])}, options give height x width {img_shape}")
         out = torch.empty((B, 1) + sino_shape, dtype=x.dtype, device=x.device)
+    elif op == N.OP_BACKPROJECTION_SV:
+        if plan.scan_type != 0:
+            raise ValueError("backprojection_sv is defined for equal-distance fan beams (scan_type 0) only")
+        if tuple(x.shape[2:]) != sino_shape:
+            raise ValueError(f"{name}: sinogram is {tuple(x.shape[2:])}, options give views x dets {sino_shape}")
+        out = torch.empty((B, plan.views) + img_shape, dtype=x.dtype, device=x.device)
     else:
         if tuple(x.shape[2:]) != sino_shape:
             raise ValueError(f"{name}: sinogram is {tuple(x.shape[2:])}, options give views x dets {sino_shape}")
@@ -201,3 +209,10 @@ def backprojection_t(image: torch.Tensor, options) -> torch.Tensor:
 def fbp(projection: torch.Tensor, options) -> torch.Tensor:
     """RL-filtered backprojection: sinogram -> image (src/ctlib.cpp:86-99)."""
     return _apply(N.OP_FBP, projection, options, "projection")
+
+
+def backprojection_sv(projection: torch.Tensor, options) -> torch.Tensor:
+    """Single-view backprojection, equal-distance fan beams only: sinogram
+    B x 1 x V x D -> B x V x H x W, image v holding view v's term of
+    backprojection (src/ctlib.cpp:45-54, src/fan_ed_kernel.cu:946-1161)."""
+    return _apply(N.OP_BACKPROJECTION_SV, projection, options, "projection")

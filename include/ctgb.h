@@ -42,7 +42,8 @@ enum {
   CTGB_OP_PROJECTION_T = 1,
   CTGB_OP_BACKPROJECTION = 2,
   CTGB_OP_BACKPROJECTION_T = 3,
-  CTGB_OP_FBP = 4
+  CTGB_OP_FBP = 4,
+  CTGB_OP_BACKPROJECTION_SV = 5
 };
 
 /* Decode an options vector (host array, the reference's layout: fan
@@ -118,6 +119,17 @@ int ctgb_backprojection_t(const ctgb_plan* plan, const void* image, void* sino, 
  * runs in TF32 unless the caller disables it). */
 int ctgb_fbp(const ctgb_plan* plan, const void* sino, void* image, int batch, void* workspace,
              size_t workspace_bytes, void* stream);
+
+/* Single-view backprojection, equal-distance fan beams only: sinogram
+ * B x 1 x V x D -> B x V x H x W, image v holding view v's term of
+ * backprojection (the same overlaps and U^2 weights, no sum over views), so that
+ * summing over views gives ctgb_backprojection. Replaces backprojection_sv():
+ * src/ctlib.cpp:45-54, bprj_sv_fan_ed_cuda and bprj_sv_fan_ed
+ * (src/fan_ed_kernel.cu:946-1161, 1299-1331). Other scan types return
+ * CTGB_ERR_INVALID (the reference exits the process). Workspace as for
+ * CTGB_OP_BACKPROJECTION_SV in ctgb_workspace_size. */
+int ctgb_backprojection_sv(const ctgb_plan* plan, const void* sino, void* images, int batch, void* workspace,
+                           size_t workspace_bytes, void* stream);
 
 /* A (as ctgb_projection) for callers that cannot allocate device memory.
  * No counterpart in the reference. Some callers of these operators may not

@@ -13,9 +13,9 @@ import numpy as np
 
 from . import build as _build
 
-OP_PRJ, OP_PRJ_T, OP_BPRJ, OP_BPRJ_T, OP_FBP, OP_RAMP = 0, 1, 2, 3, 4, 5
+OP_PRJ, OP_PRJ_T, OP_BPRJ, OP_BPRJ_T, OP_FBP, OP_RAMP, OP_BPRJ_SV = 0, 1, 2, 3, 4, 5, 6
 OP_NAMES = {"projection": OP_PRJ, "projection_t": OP_PRJ_T, "backprojection": OP_BPRJ,
-            "backprojection_t": OP_BPRJ_T, "fbp": OP_FBP}
+            "backprojection_t": OP_BPRJ_T, "fbp": OP_FBP, "backprojection_sv": OP_BPRJ_SV}
 
 # modes of oracle_run
 MODE_F32 = 0      # fp32 data and arithmetic, reference promotions
@@ -75,6 +75,8 @@ def out_shape(op: int, opts, batch: int):
     V, D, W, H = int(o[0]), int(o[1]), int(o[2]), int(o[3])
     if op in (OP_PRJ, OP_BPRJ_T):
         return (batch, 1, V, D)
+    if op == OP_BPRJ_SV:  # one image per view (fan equal-distance only)
+        return (batch, V, H, W)
     return (batch, 1, H, W)
 
 

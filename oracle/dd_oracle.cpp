@@ -32,7 +32,7 @@
 
 namespace {
 
-enum Op { OP_PRJ = 0, OP_PRJ_T = 1, OP_BPRJ = 2, OP_BPRJ_T = 3, OP_FBP = 4, OP_RAMP = 5 };
+enum Op { OP_PRJ = 0, OP_PRJ_T = 1, OP_BPRJ = 2, OP_BPRJ_T = 3, OP_FBP = 4, OP_RAMP = 5, OP_BPRJ_SV = 6 };
 enum Scan { FAN_ED = 0, FAN_EA = 1, PARA = 2 };
 
 template <class T>
@@ -272,12 +272,15 @@ void det_gather(const Opts<T>& o, const std::vector<View<T>>& views, bool transp
 // its branch, so each output pixel is written by one thread
 template <class T>
 void pix_gather(const Opts<T>& o, const std::vector<View<T>>& views, bool backproj,
-                int B, const T* sino, T* img) {
+                int B, const T* sino, T* img, bool per_view = false) {
+  // per_view: B x V x H x W output, one image per view with no sum over views
+  // (backprojection_sv, src/fan_ed_kernel.cu:946-1161 writes
+  // image[channel][view][row][col])
   const int V = o.V, D = o.D;
   const T dinterval = o.dImg / o.dDet;
   std::vector<int> xv, yv;
   for (int v = 0; v < V; ++v) (views[v].xb ? xv : yv).push_back(v);
-  std::memset(img, 0, sizeof(T) * (size_t)B * o.H * o.W);
+  std::memset(img, 0, sizeof(T) * (size_t)B * (per_view ? V : 1) * o.H * o.W);
   for (int pass = 0; pass < 2; ++pass) {
     const std::vector<int>& vl = pass == 0 ? xv : yv;
     const int nlines = pass == 0 ? o.H : o.W;
@@ -288,8 +291,8 @@ void pix_gather(const Opts<T>& o, const std::vector<View<T>>& views, bool backpr
 #pragma omp for collapse(2) schedule(dynamic, 2)
       for (int b = 0; b < B; ++b) {
         for (int line = 0; line < nlines; ++line) {
-          T* x = img + (size_t)b * o.H * o.W;
           for (int v : vl) {
+            T* x = img + ((size_t)b * (per_view ? V : 1) + (per_view ? v : 0)) * o.H * o.W;
             const View<T>& w = views[v];
             const T* y = sino + ((size_t)b * V + v) * D;
             for (int d = 0; d < D; ++d) {
@@ -433,6 +436,10 @@ int run(int op, const double* opts, int nopts, bool f32ang, int B, const void* i
     case OP_PRJ_T: pix_gather(o, views, false, B, x, y); break;
     case OP_BPRJ: pix_gather(o, views, true, B, x, y); break;
     case OP_FBP: fbp(o, views, B, x, y); break;
+    case OP_BPRJ_SV:
+      if (o.scan != FAN_ED) return 3;  // the reference defines it for equal-distance fans only
+      pix_gather(o, views, true, B, x, y, true);
+      break;
     default: return 2;
   }
   return 0;

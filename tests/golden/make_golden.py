@@ -141,16 +141,36 @@ def make(name, opts, batch, dtype, ops=OPS4 + ("fbp",)):
     print(f"{name}: {os.path.getsize(path) / 1e3:.0f} kB")
 
 
-def main():
+def single_view_cases():
+    """Single-view backprojection (fan ED only): output B x V x H x W."""
+    tp = 2 * math.pi
+    sv = ("backprojection_sv",)
+    return [
+        ("ed_single_view", fan_options(12, 40, 32, 32, 1.0, 2.0, 0.0, tp / 12, 120.0, 100.0, 0.0, FAN_ED), 1,
+         np.float32, sv),
+        # H != W, start angle and bin shift, two slices
+        ("ed_single_view_rect", fan_options(24, 61, 40, 28, 1.0, 2.0, 0.3, tp / 24, 120.0, 100.0, 0.7, FAN_ED), 2,
+         np.float32, sv),
+        # fp64, 300 bins: two 256-bin reference blocks per view
+        ("ed_single_view_f64", fan_options(16, 300, 48, 48, 1.0, 0.5, 0.1, tp / 16, 120.0, 100.0, 0.2, FAN_ED), 1,
+         np.float64, sv),
+    ]
+
+
+def main(names=None):
+    """Write every fixture, or only those named on the command line."""
+    want = (lambda n: True) if not names else (lambda n: n in names)
     for c in small_cases():
-        make(*c)
-    # single-view backprojection (fan ED only): output B x V x H x W
-    make("ed_single_view", fan_options(12, 40, 32, 32, 1.0, 2.0, 0.0, 2 * math.pi / 12, 120.0, 100.0, 0.0,
-                                       FAN_ED), 1, np.float32, ("backprojection_sv",))
+        if want(c[0]):
+            make(*c)
+    for c in single_view_cases():
+        if want(c[0]):
+            make(*c)
     for name, opts, batch, dtype in scaled_cases():
-        ops = OPS4 + ("fbp",) if name == "cfg_parallel_256" else ("projection", "projection_t", "fbp")
-        make(name, opts, batch, dtype, ops)
+        if want(name):
+            ops = OPS4 + ("fbp",) if name == "cfg_parallel_256" else ("projection", "projection_t", "fbp")
+            make(name, opts, batch, dtype, ops)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

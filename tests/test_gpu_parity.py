@@ -21,7 +21,7 @@ from conftest import GOLDEN, golden_files
 
 pytestmark = pytest.mark.gpu
 
-OPS = ("projection", "projection_t", "backprojection", "backprojection_t", "fbp")
+OPS = ("projection", "projection_t", "backprojection", "backprojection_t", "fbp", "backprojection_sv")
 
 
 @pytest.fixture(scope="module")
@@ -47,7 +47,7 @@ def _cases():
 def _ref_tol(fname, op):
     if fname.startswith("cfg_fan") and op == "projection_t":
         return 3e-4
-    if op in ("projection_t", "backprojection", "fbp"):
+    if op in ("projection_t", "backprojection", "fbp", "backprojection_sv"):
         return 3e-5
     return 1e-5
 
@@ -198,3 +198,43 @@ def test_image_gather_staged_and_global_views(ct, oracle_mod, scan, batch):
             del plan._tuned[(code, batch)]
         assert np.array_equal(two, got), op
     assert _native.wait_timeouts(0) == before
+
+
+@pytest.mark.parametrize("batch", [1, 5, 16, 19])
+def test_backprojection_sv_vs_oracle_and_sum(ct, oracle_mod, batch):
+    """Single-view backprojection (fan ED): every view's image against the FP64
+    oracle, and their sum over views against backprojection."""
+    from ctlib_gb300.workloads import FAN_ED, fan_options
+    O = oracle_mod
+    opts = fan_options(36, 70, 48, 40, 1.0, 2.0, 0.2, 2 * math.pi / 36, 120.0, 100.0, 0.4, FAN_ED)
+    rng = np.random.default_rng(200 + batch)
+    sino = rng.standard_normal((batch, 1, 36, 70)).astype(np.float32)
+    got = _run(ct, "backprojection_sv", sino, opts)
+    assert got.shape == (batch, 36, 40, 48)
+    want = O.run("backprojection_sv", sino, opts, O.MODE_F64_ON_F32)
+    assert O.rel_l2(got, want) <= 1e-5, O.rel_l2(got, want)
+    bp = _run(ct, "backprojection", sino, opts)
+    assert O.rel_l2(got.astype(np.float64).sum(axis=1, keepdims=True), bp) <= 1e-6
+
+
+def test_backprojection_sv_full_size_sums_to_backprojection(ct):
+    """Headline geometry (512^2, 1152 views, 736 bins), 2 slices: 2.4 GB of
+    per-view images whose sum over views is backprojection."""
+    from ctlib_gb300.workloads import fan_ed_512
+    o = torch.tensor(fan_ed_512(1).slices[0].options, dtype=torch.float32)
+    g = torch.Generator().manual_seed(11)
+    y = torch.randn(2, 1, 1152, 736, generator=g).cuda()
+    sv = ct.backprojection_sv(y, o)
+    assert sv.shape == (2, 1152, 512, 512)
+    s = sv.double().sum(dim=1, keepdim=True)
+    del sv
+    bp = ct.backprojection(y, o).double()
+    err = float((s - bp).norm() / bp.norm())
+    assert err <= 1e-6, err
+
+
+def test_backprojection_sv_rejects_other_geometries(ct):
+    from ctlib_gb300.workloads import FAN_EA, fan_options
+    opts = torch.tensor(fan_options(8, 20, 16, 16, 1.0, 0.01, 0.0, 0.5, 120.0, 100.0, 0.0, FAN_EA))
+    with pytest.raises(ValueError):
+        ct.backprojection_sv(torch.zeros(1, 1, 8, 20, device="cuda"), opts)

@@ -21,7 +21,7 @@ import pytest
 
 from conftest import GOLDEN, golden_files
 
-OPS = ("projection", "projection_t", "backprojection", "backprojection_t", "fbp")
+OPS = ("projection", "projection_t", "backprojection", "backprojection_t", "fbp", "backprojection_sv")
 
 
 def _cases():
@@ -115,3 +115,23 @@ def test_adjoint_pairs_fp64(oracle_mod):
             By = O.run("backprojection", y, o, O.MODE_F64)
             lhs, rhs = float((Bty * y).sum()), float((x * By).sum())
             assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0), (o[-1], lhs, rhs)
+
+
+@pytest.mark.parametrize("fname", [f for f in golden_files() if "backprojection_sv_in" in np.load(f"{GOLDEN}/{f}")])
+def test_single_view_backprojection_sums_to_backprojection(oracle_mod, fname):
+    """backprojection_sv is backprojection before its sum over views: summing
+    its B x V x H x W output over views gives backprojection."""
+    O = oracle_mod
+    z = np.load(f"{GOLDEN}/{fname}")
+    x = z["backprojection_sv_in"].astype(np.float64)
+    sv = O.run("backprojection_sv", x, z["options"], O.MODE_F64)
+    bp = O.run("backprojection", x, z["options"], O.MODE_F64)
+    assert sv.shape == (x.shape[0], x.shape[2], bp.shape[2], bp.shape[3])
+    assert O.rel_l2(sv.sum(axis=1, keepdims=True), bp) <= 1e-13
+
+
+def test_single_view_backprojection_fan_ed_only(oracle_mod):
+    from ctlib_gb300.workloads import FAN_EA, fan_options
+    opts = fan_options(8, 20, 16, 16, 1.0, 0.01, 0.0, 0.5, 120.0, 100.0, 0.0, FAN_EA)
+    with pytest.raises(ValueError):
+        oracle_mod.run("backprojection_sv", np.zeros((1, 1, 8, 20)), opts, oracle_mod.MODE_F64)
