@@ -250,13 +250,27 @@ __device__ __forceinline__ void prefetch_tables(const PrefetchList& L) {
 // ----------------------------------------------------------------------------
 // layout kernels
 // ----------------------------------------------------------------------------
-// image [B][H][W] -> row lines [G][H][NQ][W][QW] and column lines
-// [G][W][NQ][H][QW] (column walk index k = H-1-row), zero-padded to G*SB slices
+// Pixel-blocked line layout of the detector gather: a line is a run of blocks
+// of 8 pixels, each block holding the block's NQ planes of 8 x QW values, so the
+// planes of pixel k lie at fixed offsets (qd * 8 * QW) from blk_off(k) and the
+// lanes of a warp, which read consecutive pixels, still read whole 128-byte
+// lines. With one plane (SB = 1) the layout is the plain row [N].
+template <int SB>
+__host__ __device__ __forceinline__ int blk_off(int k) {
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+  return ((k >> 3) * NQ * 8 + (k & 7)) * QW;
+}
+__host__ __device__ __forceinline__ int round8(int n) { return (n + 7) & ~7; }
+
+// image [B][H][W] -> row lines [G][H][blocked W] and column lines [G][W][blocked
+// H] (column walk index k = H-1-row), zero-padded to G*SB slices; a line holds
+// round8(N) * SB values
 template <class T, int SB>
 __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T* __restrict__ imy, int B,
                                int H, int W, int G, PrefetchList pf) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   prefetch_tables(pf);
+  const size_t sx = (size_t)round8(W) * SB, sy = (size_t)round8(H) * SB;
   const size_t n = (size_t)G * NQ * H * W;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % W);
@@ -269,8 +283,8 @@ __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T
       const int b = g * SB + qd * QW + j;
       v[j] = b < B ? img[((size_t)b * H + r) * W + c] : T(0);
     }
-    store_q<T, QW>(imx + ((((size_t)g * H + r) * NQ + qd) * W + c) * QW, v);
-    store_q<T, QW>(imy + ((((size_t)g * W + c) * NQ + qd) * H + (H - 1 - r)) * QW, v);
+    store_q<T, QW>(imx + ((size_t)g * H + r) * sx + blk_off<SB>(c) + qd * 8 * QW, v);
+    store_q<T, QW>(imy + ((size_t)g * W + c) * sy + blk_off<SB>(H - 1 - r) + qd * 8 * QW, v);
   }
 }
 
@@ -329,13 +343,17 @@ __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
 // and the cell spans [f, f + w/sigma) pixels from k on.
 template <class T, int SB, int KIND, int U>
 __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int d, int g, const T* __restrict__ imx,
-                                                const T* __restrict__ imy, T* __restrict__ out, int B) {
+                                                const T* __restrict__ imy, size_t sx_line, size_t sy_line,
+                                                T* __restrict__ out, int B) {
+  // row lines of slice group g start at imx + g*H*sx_line, column lines at
+  // imy + g*W*sy_line; a line is pixel-blocked (blk_off)
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   const int fl = P.flags[v];
   const bool xb = fl & 1;
   const int nlines = xb ? P.H : P.W;
   const int N = xb ? P.W : P.H;
-  const T* base = (xb ? imx : imy) + (size_t)g * P.H * P.W * SB;
+  const size_t stride = xb ? sx_line : sy_line;
+  const T* base = xb ? imx + (size_t)g * P.H * sx_line : imy + (size_t)g * P.W * sy_line;
   const size_t bi = ((size_t)v * (P.D + 1) + d) * 2;
   const T Dh = P.db2[bi], Dl = P.db2[bi + 1];
   const T wcell = P.wd[(size_t)v * P.D + d];
@@ -380,10 +398,13 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
       continue;
     }
-    const T* row = base + (size_t)l * N * SB;
+    // pixels past the line's end take no weight: with b clamped to N - k their
+    // overlaps come out <= 0 (the clamp is exact, N - k is an integer)
+    b = fmin(b, T(N - k));
+    const T* row = base + (size_t)l * stride;
     T lc = T(0);
     if (KIND == kBt && P.scan != kPara) lc = xb ? P.rowc[l] : P.colc[l];
-    // weight of pixel k (overlap ov in pixel units)
+    // weight of pixel kk (overlap ov in pixel units, ov >= 0)
     auto weight = [&](T ov, int kk) {
       T w = ov;
       if (KIND == kA) {
@@ -397,41 +418,40 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       }
       return w;
     };
-    // first U pixels straight-line: all overlaps, then all loads, then
-    // all FMAs (steps past the cell or the image get weight 0 on a clamped,
-    // valid pixel), so the loads of one line are in flight together
+    // first U pixels straight-line: all overlaps, then all loads, then all
+    // FMAs (steps past the cell or the line get weight 0 on a clamped, valid
+    // pixel), so the loads of one line are in flight together. The overlap of
+    // pixel k+j is min(b-j, 1) - max(a-j, 0); a < 2, so from j = 2 on the
+    // second term is 0.
     T wj[U];
-    int kj[U];
+    int oj[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) {
-      const T aj = a - T(j), bj = b - T(j);
-      T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
-      const bool inside = k + j < N;
-      if (!(ov > T(0)) || !inside) ov = T(0);
-      kj[j] = inside ? k + j : N - 1;
-      wj[j] = ov > T(0) ? weight(ov, kj[j]) : T(0);
+      const T hi = fmin(b - T(j), T(1));
+      const T ov = j < 2 ? hi - fmax(a - T(j), T(0)) : hi;
+      const int kk = min(k + j, N - 1);
+      oj[j] = blk_off<SB>(kk);
+      wj[j] = ov > T(0) ? weight(ov, kk) : T(0);
     }
 #pragma unroll
     for (int qd = 0; qd < NQ; ++qd) {
       T u[U][QW];
 #pragma unroll
-      for (int j = 0; j < U; ++j) load_q<T, QW>(row + ((size_t)qd * N + kj[j]) * QW, u[j]);
+      for (int j = 0; j < U; ++j) load_q<T, QW>(row + oj[j] + qd * 8 * QW, u[j]);
 #pragma unroll
       for (int j = 0; j < U; ++j)
 #pragma unroll
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(wj[j], u[j][i], blk[qd * QW + i]);
     }
     // rare: a cell wider than U - 1 pixels
-    for (int j = U; b - T(j) > T(0) && k + j < N; ++j) {
-      const T aj = a - T(j), bj = b - T(j);
-      const T ov = (bj < T(1) ? bj : T(1)) - (aj > T(0) ? aj : T(0));
-      if (!(ov > T(0))) continue;
+    for (int j = U; b - T(j) > T(0); ++j) {
+      const T ov = fmin(b - T(j), T(1));
       const T w = weight(ov, k + j);
-      const T* px = row + (size_t)(k + j) * QW;
+      const T* px = row + blk_off<SB>(k + j);
 #pragma unroll
       for (int qd = 0; qd < NQ; ++qd) {
         T u[QW];
-        load_q<T, QW>(px + (size_t)qd * N * QW, u);
+        load_q<T, QW>(px + qd * 8 * QW, u);
 #pragma unroll
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(w, u[i], blk[qd * QW + i]);
       }
@@ -457,7 +477,8 @@ __global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __res
   const int d = blockIdx.x * 32 + lane;
   const int v = blockIdx.y * (blockDim.x >> 5) + warp;
   if (v >= P.V || d >= P.D) return;
-  det_gather_cell<T, SB, KIND, U>(P, v, d, blockIdx.z, imx, imy, out, B);
+  det_gather_cell<T, SB, KIND, U>(P, v, d, blockIdx.z, imx, imy, (size_t)round8(P.W) * SB,
+                                  (size_t)round8(P.H) * SB, out, B);
 }
 
 // ----------------------------------------------------------------------------
@@ -1183,7 +1204,7 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   const size_t es = esize(p->dtype);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
-    return 2 * al(G * g.H * g.W * sb * es);
+    return al(G * g.H * (size_t)round8(g.W) * sb * es) + al(G * g.W * (size_t)round8(g.H) * sb * es);
   return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
 }
 
@@ -1201,7 +1222,7 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
   T* y = static_cast<T*>(out);
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
     T* imx = static_cast<T*>(ws);
-    T* imy = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + al((size_t)G * g.H * g.W * SB * sizeof(T)));
+    T* imy = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + al((size_t)G * g.H * round8(g.W) * SB * sizeof(T)));
     const size_t n = (size_t)G * g.H * g.W;
     const int tb = 256;
     const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
@@ -1375,7 +1396,8 @@ __global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<float>* __
     const int v = tk.a * (blockDim.x >> 5) + warp, d = tk.b * 32 + lane;
     if (v < P.V && d < P.D)
       det_gather_cell<float, 1, KIND, 3>(P, v, d, 0, io.in[tk.slice],
-                                      reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice], 1);
+                                      reinterpret_cast<const float*>(ws + off[tk.slice]), (size_t)P.W,
+                                      (size_t)P.H, io.out[tk.slice], 1);
   }
 }
 
