@@ -611,13 +611,25 @@ __device__ __forceinline__ int seed_cell(int scan, float xf, const Seed& sd, int
   return (int)fminf(fmaxf(cb, (float)dlo), (float)(dhi - 1));
 }
 
-// one view's contribution to one pixel (lower edge index k on its line, line
-// map A4), accumulated into blk; U cells straight-line, then the remainder
-template <class T, int SB, int KIND, int U, bool SM>
-__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
-                                         T pcx, T pcy, const T* __restrict__ rec, const T* __restrict__ qv, int qs,
-                                         int base, int dlo, int dhi, T (&blk)[SB]) {
-  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
+// Where one view meets one pixel: the pixel's first U cells (offsets oj from
+// `base`, overlap weights ov) and the state the remainder loop resumes from.
+template <class T, int U>
+struct CellSpan {
+  int d;     // first cell after the straight-line ones
+  T a, b;    // pixel edges relative to cell d's lower boundary
+  T wv;      // backprojector view weight
+  T ov[U];
+  int oj[U];
+};
+
+// Geometry of one view for one pixel (lower edge index k on its line, line
+// map A4): exact edge, seeded and corrected cell search, U straight-line
+// overlaps (cells past the pixel or the range get weight 0 on a clamped, valid
+// cell).
+template <class T, int KIND, int U, bool SM>
+__device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
+                                         T pcx, T pcy, const T* __restrict__ rec, int base, int dlo, int dhi,
+                                         CellSpan<T, U>& cs) {
   const T kf = T(k);
   // x = alpha + sigma*k as (xs, xl)
   const T qh = mul_rn(A4.z, kf);
@@ -658,35 +670,44 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
     else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(sx, sy, pcx, pcy) * sig);
     else wv = T(1) / P.dImg;
   }
-  // first U cells straight-line (cells past the pixel or the range get weight
-  // 0 on a clamped, valid cell), then the rare remainder
-  T ovj[U];
-  int oj[U];
 #pragma unroll
   for (int j = 0; j < U; ++j) {
     const bool inside = d + j < dhi;
-    oj[j] = (inside ? d + j : dhi - 1) - base;
-    const T w = j == 0 ? w0 : rec[oj[j] * 4 + 2];
+    cs.oj[j] = (inside ? d + j : dhi - 1) - base;
+    const T w = j == 0 ? w0 : rec[cs.oj[j] * 4 + 2];
     T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-    ovj[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
+    cs.ov[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
     a -= w;
     b -= w;
   }
+  cs.d = d + U;
+  cs.a = a;
+  cs.b = b;
+  cs.wv = wv;
+}
+
+// The sums of one view's span into blk: U straight-line cells, then the rare
+// remainder (cells past the U-th one that the pixel still reaches)
+template <class T, int SB, int KIND, int U, bool SM>
+__device__ __forceinline__ void pix_accum(const CellSpan<T, U>& cs, const T* __restrict__ rec,
+                                          const T* __restrict__ qv, int qs, int base, int dhi, T (&blk)[SB]) {
+  constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
 #pragma unroll
   for (int qd = 0; qd < NQ; ++qd) {
     T qq[U][QW];
 #pragma unroll
-    for (int j = 0; j < U; ++j) ldq<T, QW, SM>(qv + (qd * qs + oj[j]) * QW, qq[j]);
+    for (int j = 0; j < U; ++j) ldq<T, QW, SM>(qv + (qd * qs + cs.oj[j]) * QW, qq[j]);
 #pragma unroll
     for (int j = 0; j < U; ++j)
 #pragma unroll
-      for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(ovj[j], qq[j][i], blk[qd * QW + i]);
+      for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(cs.ov[j], qq[j][i], blk[qd * QW + i]);
   }
-  for (d += U; b > T(0) && d < dhi; ++d) {
+  T a = cs.a, b = cs.b;
+  for (int d = cs.d; b > T(0) && d < dhi; ++d) {
     const T w = rec[(d - base) * 4 + 2];
     T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
     if (ov > T(0)) {
-      if (KIND == kB) ov *= wv;
+      if (KIND == kB) ov *= cs.wv;
 #pragma unroll
       for (int qd = 0; qd < NQ; ++qd) {
         T qq[QW];
@@ -700,6 +721,16 @@ __device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4,
   }
 }
 
+// one view's contribution to one pixel, accumulated into blk
+template <class T, int SB, int KIND, int U, bool SM>
+__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
+                                         T pcx, T pcy, const T* __restrict__ rec, const T* __restrict__ qv, int qs,
+                                         int base, int dlo, int dhi, T (&blk)[SB]) {
+  CellSpan<T, U> cs;
+  pix_geom<T, KIND, U, SM>(P, A4, k, sd, sx, sy, pcx, pcy, rec, base, dlo, dhi, cs);
+  pix_accum<T, SB, KIND, U, SM>(cs, rec, qv, qs, base, dhi, blk);
+}
+
 // view v of pixel (r, c), everything read from the global tables; q planes of
 // view v start at qv with stride qs
 template <class T, int SB, int KIND, int U>
@@ -711,6 +742,13 @@ __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int 
   pix_view<T, SB, KIND, U, false>(P, A4, k, load_seed(P.inv + (size_t)v * 5), P.src[2 * v], P.src[2 * v + 1], pcx,
                                   pcy, P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
 }
+
+// Parts per tile of the staged image gather: two view halves whenever there are
+// enough views. Halving every tile's CTA time fills the last wave of grids that
+// are only a few waves deep. The split depends on V alone, never on the launch
+// schedule, so every schedule still gives the same result bit for bit; the
+// ragged path sums the same halves and matches too.
+__host__ __device__ __forceinline__ int view_split(int views) { return views >= 64 ? 2 : 1; }
 
 // Staged image gather. A CTA is a 32 x R pixel tile (R consumer warps, lane =
 // column, warp = row) plus one producer warp. For each view the producer finds
@@ -737,9 +775,16 @@ struct PixSlot {
 
 // SV: single-view backprojection (src/fan_ed_kernel.cu:946-1161): each view's
 // sum goes to its own image, img[slice][view][row][col], with no sum over views.
+//
+// nsplit (1 or 2): blockIdx.z = slice group * nsplit + part, and part p sums
+// views [V*p/nsplit, V*(p+1)/nsplit). With two parts each adds its scaled sum
+// into the zeroed output with one atomic add; 0 + a + b is the same in either
+// order, so the result is deterministic. Shorter CTAs fill the last wave of a
+// grid that is only a few waves deep.
 template <class T, int SB, int KIND, int U, bool SV = false>
 __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
-                                                       T* __restrict__ img, int B, T out_mul, T out_div) {
+                                                       T* __restrict__ img, int B, T out_mul, T out_div,
+                                                       int nsplit) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
@@ -754,8 +799,11 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][blockDim]: running sum, compensation
   unsigned char* slots = pix_smem + (size_t)2 * SB * blockDim.x * sizeof(T);
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R, g = blockIdx.z;
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R;
+  const int part = blockIdx.z % nsplit, g = blockIdx.z / nsplit;
   const int V = P.V, D = P.D, Dp = P.Dp;
+  const int vbeg = (int)((long long)V * part / nsplit), vend = (int)((long long)V * (part + 1) / nsplit);
+  const int NV = vend - vbeg;  // views of this CTA; the slot of view vbeg + u is u % kSlots
   const T* qg = q + (size_t)g * V * Dp * SB;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kSlots; ++i) {
@@ -781,7 +829,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
     };
     auto load_in = [&](int v, ViewIn& in) {
       in.fl = 0;
-      if (v >= V) return;
+      if (v >= vend) return;
       in.fl = P.flags[v];
       in.sd = load_seed(P.inv + (size_t)v * 5);
       in.sx = P.src[2 * v];
@@ -792,7 +840,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
     };
     // window start of view v, or -1 if the tile's footprint does not fit
     auto window = [&](int v, const ViewIn& in, int& l0, int& nl) {
-      if (v >= V) return -1;
+      if (v >= vend) return -1;
       const bool xb = in.fl & 1;
       int ka, kb;
       if (xb) { ka = c0; kb = c1 + 1; l0 = r0; nl = r1 - r0 + 1; }
@@ -827,13 +875,13 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
     };
     ViewIn cur, nxt;
     int ws, l0 = 0, nl = 0;
-    load_in(lane, cur);
-    ws = window(lane, cur, l0, nl);
-    for (int vb = 0; vb < V; vb += 32) {
-      load_in(vb + 32 + lane, nxt);  // in flight during this batch's copies
-      const int nv = min(32, V - vb);
+    load_in(vbeg + lane, cur);
+    ws = window(vbeg + lane, cur, l0, nl);
+    for (int ub = 0; ub < NV; ub += 32) {
+      load_in(vbeg + ub + 32 + lane, nxt);  // in flight during this batch's copies
+      const int nv = min(32, NV - ub);
       for (int j = 0; j < nv; ++j) {
-        const int vj = vb + j, slot = vj % kSlots, use = vj / kSlots;
+        const int vj = vbeg + ub + j, slot = (ub + j) % kSlots, use = (ub + j) / kSlots;
         if (lane == 0 && use > 0 && !ld_volatile(s_bad)) {
           if (!mbar_wait(&s_empty[slot], (use - 1) & 1)) report_timeout(&s_bad);
         }
@@ -870,13 +918,13 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
           bulk_g2s(sl + S::kQBytes + S::kRecBytes, P.lp + ((size_t)vj * P.L + l0j) * 4, lbytes, &s_full[slot]);
       }
       cur = nxt;
-      ws = window(vb + 32 + lane, cur, l0, nl);
+      ws = window(vbeg + ub + 32 + lane, cur, l0, nl);
     }
     // Normally the consumers have waited on every phase issued. After a wait
     // ran out, make sure no copy is still landing in this CTA's shared memory.
     if (lane == 0 && ld_volatile(s_bad)) {
-      for (int i = 0; i < kSlots && i < V; ++i) {
-        const int last = i + ((V - 1 - i) / kSlots) * kSlots;
+      for (int i = 0; i < kSlots && i < NV; ++i) {
+        const int last = i + ((NV - 1 - i) / kSlots) * kSlots;
         mbar_wait(&s_full[i], (last / kSlots) & 1);
       }
     }
@@ -892,11 +940,11 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
   T blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) blk[s] = T(0);
-  for (int v = 0; v < V; ++v) {
-    const int slot = v % kSlots;
+  for (int u = 0; u < NV; ++u) {
+    const int v = vbeg + u, slot = u % kSlots;
     bool ok = false;
     if (!ld_volatile(s_bad)) {
-      ok = mbar_wait(&s_full[slot], (v / kSlots) & 1);
+      ok = mbar_wait(&s_full[slot], (u / kSlots) & 1);
       if (!ok) report_timeout(&s_bad);
     }
     if (SV) {
@@ -933,7 +981,7 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
           if (bb < B) img[(((size_t)bb * V + v) * P.H + r) * P.W + c] = blk[s];
         }
       }
-    } else if ((v % kFoldEvery) == kFoldEvery - 1) {
+    } else if ((u % kFoldEvery) == kFoldEvery - 1) {
       kahan_fold_smem<T, SB>(acc, blk);
     }
   }
@@ -943,7 +991,11 @@ __global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
-    if (bb < B) img[((size_t)bb * P.H + r) * P.W + c] = acc[(size_t)s * blockDim.x + threadIdx.x] * out_mul / out_div;
+    if (bb >= B) continue;
+    const T val = acc[(size_t)s * blockDim.x + threadIdx.x] * out_mul / out_div;
+    T* dst = img + ((size_t)bb * P.H + r) * P.W + c;
+    if (nsplit == 1) *dst = val;
+    else atomicAdd(dst, val);
   }
 }
 
@@ -957,14 +1009,21 @@ __device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int 
   const bool active = c < P.W && r < P.H;
   if (!active) return;
   const T pcx = P.colc[c], pcy = P.rowc[r];
-  kahan_init_smem<T, 1>(acc);
-  T blk[1] = {T(0)};
-  for (int v = 0; v < P.V; ++v) {
-    pix_view_global<T, 1, KIND, 3>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
-    if ((v % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk);
+  // the same view parts, fold points and final additions as k_pix_gather
+  const int nsplit = view_split(P.V);
+  T out = T(0);
+  for (int part = 0; part < nsplit; ++part) {
+    const int vbeg = (int)((long long)P.V * part / nsplit), vend = (int)((long long)P.V * (part + 1) / nsplit);
+    kahan_init_smem<T, 1>(acc);
+    T blk[1] = {T(0)};
+    for (int v = vbeg; v < vend; ++v) {
+      pix_view_global<T, 1, KIND, 3>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
+      if (((v - vbeg) % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk);
+    }
+    kahan_fold_smem<T, 1>(acc, blk);
+    out += acc[threadIdx.x] * out_mul / out_div;
   }
-  kahan_fold_smem<T, 1>(acc, blk);
-  img[(size_t)r * P.W + c] = acc[threadIdx.x] * out_mul / out_div;
+  img[(size_t)r * P.W + c] = out;
 }
 
 // ----------------------------------------------------------------------------
@@ -1281,8 +1340,13 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
     auto launch = [&](auto kern, T mul, T div) -> int {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
+      const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? 1 : view_split(g.V);
+      if (nsplit > 1) {
+        e = cudaMemsetAsync(y, 0, (size_t)batch * g.H * g.W * sizeof(T), st);
+        if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather clear: ") + cudaGetErrorString(e));
+      }
       if (p->ev_start) cudaEventRecord(p->ev_start, st);
-      kern<<<grid, nt, smem, st>>>(P, qb, y, batch, mul, div);
+      kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, batch, mul, div, nsplit);
       if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
       return CTGB_OK;
     };
