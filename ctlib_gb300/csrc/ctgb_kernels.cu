@@ -18,7 +18,7 @@
 // Slices are processed SB at a time per thread (geometry computed once, SB
 // fused multiply-adds per overlap); inputs are first re-laid out so that the
 // SB values of one pixel / cell are one vector load. Sums over lines and views
-// use blocked Kahan compensation (plain fp32 within a block of 16, compensated
+// use blocked Kahan compensation (plain fp32 within a block of 32, compensated
 // across blocks). The RL ramp filter of fbp is a direct convolution with the
 // odd-tap structure of the RL kernel, fused with the detector pre-weight.
 //
@@ -206,7 +206,7 @@ __device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)
 }
 
 enum Kind { kA = 0, kBt = 1, kAt = 2, kB = 3 };
-constexpr int kFoldEvery = 16;
+constexpr int kFoldEvery = 32;
 // Straight-line pixels per cell (cells per pixel) before the remainder loop: U
 // = 3 or 2 per operator (ctgb_plan_set_unroll), 3 unless tuned.
 
