@@ -763,7 +763,7 @@ __host__ __device__ __forceinline__ int view_split(int views) { return views >= 
 // a pixel can reach (including the seed correction and the step back when the
 // offset is negative) lies inside it.
 constexpr int kWin = 64;   // cells per staged view window (multiple of 4)
-constexpr int kSlots = 8;  // views in flight per CTA
+constexpr int kSlots = 6;  // views in flight per CTA
 
 template <class T, int SB>
 struct PixSlot {
@@ -782,7 +782,7 @@ struct PixSlot {
 // order, so the result is deterministic. Shorter CTAs fill the last wave of a
 // grid that is only a few waves deep.
 template <class T, int SB, int KIND, int U, bool SV = false>
-__global__ void __launch_bounds__(288, 2) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
+__global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div,
                                                        int nsplit) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
