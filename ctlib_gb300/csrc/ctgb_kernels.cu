@@ -471,7 +471,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
 }
 
 template <class T, int SB, int KIND, int U>
-__global__ void __launch_bounds__(256) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
+__global__ void __maxnreg__(72) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
                                                     const T* __restrict__ imy, T* __restrict__ out, int B) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
