@@ -26,6 +26,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 OK, ERR_INVALID, ERR_CUDA, ERR_WORKSPACE = 0, 1, 2, 3
 OP_PROJECTION, OP_PROJECTION_T, OP_BACKPROJECTION, OP_BACKPROJECTION_T, OP_FBP = 0, 1, 2, 3, 4
 OP_BACKPROJECTION_SV = 5
+OP_DATA_GRADIENT = 6  # workspace queries of ctgb_data_gradient
 
 _lock = threading.Lock()
 _lib = None
@@ -86,6 +87,8 @@ def _declare(l):
         f = getattr(l, name)
         f.argtypes = [vp, vp, vp, c_int, vp, c_size, vp]
         f.restype = c_int
+    l.ctgb_data_gradient.argtypes = [vp, vp, vp, vp, vp, c_int, vp, c_size, vp]
+    l.ctgb_data_gradient.restype = c_int
     l.ctgb_projection_noalloc.argtypes = [vp, vp, vp, c_int, vp]
     l.ctgb_projection_noalloc.restype = c_int
     l.ctgb_projection_noalloc_max_bytes.argtypes = []
@@ -141,7 +144,7 @@ EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_pla
             "ctgb_plan_set_kernel_events",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
-            "ctgb_fbp", "ctgb_backprojection_sv", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
+            "ctgb_fbp", "ctgb_backprojection_sv", "ctgb_data_gradient", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
             "ctgb_ragged_destroy", "ctgb_ragged_workspace_size", "ctgb_ragged_run", "ctgb_last_error",
             "ctgb_version", "ctgb_geometry_query", "ctgb_wait_timeouts")
 

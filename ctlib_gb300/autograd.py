@@ -5,6 +5,8 @@ backward runs the hand-written adjoint kernel.
 * ``ProjectorT``: x = A^T y, backward A g
 * ``Backprojector``: x = B y, backward B^T g       (backprojection <-> backprojection_t)
 * ``BackprojectorT``: y = B^T x, backward B g
+* ``data_fidelity(x, y, options)``: 0.5*||A x - y||^2, whose forward computes the
+  residual and A^T(A x - y) in one fused library call
 
 For equal-angle fan geometry the reference's backprojection_t carries an extra
 dImg/cbar factor (src/fan_ea_kernel.cu:590-607) and is therefore not the exact
@@ -101,3 +103,29 @@ class Backprojector(_Module):
 
 class BackprojectorT(_Module):
     _fn = staticmethod(backprojection_t)
+
+
+class _DataFidelity(torch.autograd.Function):
+    """0.5*||A x - y||^2 summed over the batch. The forward pass computes the
+    residual and the gradient A^T(A x - y) in one library call
+    (ctgb_data_gradient); backward only scales them."""
+
+    @staticmethod
+    def forward(ctx, x, y, options):
+        from .ops import data_gradient
+        grad, res = data_gradient(x.detach(), y.detach(), options, return_residual=True)
+        ctx.save_for_backward(grad, res)
+        return 0.5 * (res.double() * res.double()).sum().to(x.dtype)
+
+    @staticmethod
+    def backward(ctx, g):
+        grad, res = ctx.saved_tensors
+        gx = g * grad if ctx.needs_input_grad[0] else None
+        gy = -g * res if ctx.needs_input_grad[1] else None
+        return gx, gy, None
+
+
+def data_fidelity(x, y, options):
+    """0.5*||A x - y||^2 for an image batch x and measured sinograms y, with
+    d/dx = A^T(A x - y) and d/dy = -(A x - y) from one fused call."""
+    return _DataFidelity.apply(x, y, options)

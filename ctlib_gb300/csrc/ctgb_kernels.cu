@@ -341,10 +341,22 @@ __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
 // pixel-edge units is u = db*(1/sigma) + beta; it is split into an integer
 // anchor k and a fraction f computed from exact products (two-product via FMA),
 // and the cell spans [f, f + w/sigma) pixels from k on.
-template <class T, int SB, int KIND, int U>
+// Residual epilogue of the data-term gradient (RES): r = A x - y for the
+// measured sinogram y (B x V x D), written to `res` (same layout, may be null)
+// and, times the A^T factor fq, straight into the image gather's input layout
+// q[G][V][NQ][Dp][QW] (increasing-boundary cell order), so A^T(Ax - y) needs no
+// separate subtraction or re-layout of the sinogram.
+template <class T>
+struct ResidualOut {
+  const T* y;
+  T* res;
+  T* q;
+};
+
+template <class T, int SB, int KIND, int U, bool RES = false>
 __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int d, int g, const T* __restrict__ imx,
                                                 const T* __restrict__ imy, size_t sx_line, size_t sy_line,
-                                                T* __restrict__ out, int B) {
+                                                T* __restrict__ out, int B, ResidualOut<T> ro = {}) {
   // row lines of slice group g start at imx + g*H*sx_line, column lines at
   // imy + g*W*sy_line; a line is pixel-blocked (blk_off)
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
@@ -463,22 +475,44 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
   if (KIND == kA) fac = P.fq[(size_t)v * P.D + d];
   else if (P.scan == kFanEA) fac = P.fbt[(size_t)v * P.D + d];
   const int de = (fl & 2) ? P.D - 1 - d : d;
+  if constexpr (RES) {
+    constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
 #pragma unroll
-  for (int s = 0; s < SB; ++s) {
-    const int bb = g * SB + s;
-    if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = acc[(size_t)s * blockDim.x + threadIdx.x] * fac;
+    for (int qd = 0; qd < NQ; ++qd) {
+      T vals[QW];
+#pragma unroll
+      for (int i = 0; i < QW; ++i) {
+        const int s = qd * QW + i, bb = g * SB + s;
+        T r = T(0);
+        if (bb < B) {
+          const size_t e = ((size_t)bb * P.V + v) * P.D + de;
+          // rounded as projection's output, then the subtraction (no contraction)
+          r = sub_rn(mul_rn(acc[(size_t)s * blockDim.x + threadIdx.x], fac), ro.y[e]);
+          if (ro.res) ro.res[e] = r;
+        }
+        vals[i] = mul_rn(r, fac);
+      }
+      store_q<T, QW>(ro.q + ((((size_t)g * P.V + v) * NQ + qd) * P.Dp + d) * QW, vals);
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < SB; ++s) {
+      const int bb = g * SB + s;
+      if (bb < B) out[((size_t)bb * P.V + v) * P.D + de] = acc[(size_t)s * blockDim.x + threadIdx.x] * fac;
+    }
   }
 }
 
-template <class T, int SB, int KIND, int U>
+template <class T, int SB, int KIND, int U, bool RES = false>
 __global__ void __maxnreg__(72) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
-                                                    const T* __restrict__ imy, T* __restrict__ out, int B) {
+                                                    const T* __restrict__ imy, T* __restrict__ out, int B,
+                                                    ResidualOut<T> ro) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
   const int v = blockIdx.y * (blockDim.x >> 5) + warp;
   if (v >= P.V || d >= P.D) return;
-  det_gather_cell<T, SB, KIND, U>(P, v, d, blockIdx.z, imx, imy, (size_t)round8(P.W) * SB,
-                                  (size_t)round8(P.H) * SB, out, B);
+  det_gather_cell<T, SB, KIND, U, RES>(P, v, d, blockIdx.z, imx, imy, (size_t)round8(P.W) * SB,
+                                       (size_t)round8(P.H) * SB, out, B, ro);
 }
 
 // ----------------------------------------------------------------------------
@@ -1271,99 +1305,159 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
 template <class T, int SB>
 constexpr bool kTwoStep = sizeof(T) == 4 && SB >= 4;
 
-template <class T, int SB>
-static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* in, void* out, int batch,
-                  void* ws, cudaStream_t st) {
+// bytes of the image line planes of the detector gather, and of the sinogram
+// planes of the image gather, for G slice groups of SB slices
+static size_t det_planes_bytes(const HostGeom& g, size_t G, int sb, size_t es) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  return al(G * g.H * (size_t)round8(g.W) * sb * es) + al(G * g.W * (size_t)round8(g.H) * sb * es);
+}
+static size_t pix_planes_bytes(const HostGeom& g, size_t G, int sb, size_t es) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
+}
+
+// The data-term gradient groups slices as projection_t does (both gathers read
+// planes of the same grouping); its workspace holds both plane sets.
+static int gradient_sb(const ctgb_plan* p, int batch) {
+  return slices_per_thread(p->dtype, batch, p->sb_cap[CTGB_OP_PROJECTION_T]);
+}
+static size_t gradient_workspace_bytes(const ctgb_plan* p, int batch) {
+  const int sb = gradient_sb(p, batch);
+  const size_t G = (size_t)((batch + sb - 1) / sb);
+  return det_planes_bytes(p->geom, G, sb, esize(p->dtype)) + pix_planes_bytes(p->geom, G, sb, esize(p->dtype));
+}
+
+// Image re-layout + detector gather: A or B^T of x into y, or (RES) A's residual
+// against ro.y for the data-term gradient. `sched` is the operator whose
+// schedule (warps per CTA, straight-line steps) is used.
+template <class T, int SB, bool RES>
+static int launch_det(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, const T* x, T* y, int batch,
+                      void* ws, cudaStream_t st, ResidualOut<T> ro = {}) {
   const int G = (batch + SB - 1) / SB;
   const HostGeom& g = p->geom;
-  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const T* x = static_cast<const T*>(in);
-  T* y = static_cast<T*>(out);
-  if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
-    T* imx = static_cast<T*>(ws);
-    T* imy = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + al((size_t)G * g.H * round8(g.W) * SB * sizeof(T)));
-    const size_t n = (size_t)G * g.H * g.W;
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  T* imx = static_cast<T*>(ws);
+  T* imy = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + al((size_t)G * g.H * round8(g.W) * SB * sizeof(T)));
+  const size_t n = (size_t)G * g.H * g.W;
+  const int tb = 256;
+  const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
+  PrefetchList pf{};
+  const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
+  pf.ptr[0] = P.lg; pf.bytes[0] = VL * 4 * sizeof(T);
+  pf.ptr[1] = P.ls; pf.bytes[1] = VL * sizeof(T);
+  pf.ptr[2] = P.db2; pf.bytes[2] = (VD + g.V) * 2 * sizeof(T);
+  pf.ptr[3] = P.wd; pf.bytes[3] = VD * sizeof(T);
+  pf.ptr[4] = op == CTGB_OP_BACKPROJECTION_T ? P.fbt : P.fq; pf.bytes[4] = VD * sizeof(T);
+  pf.n = 5;
+  k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G, pf);
+  const int wpc = p->warps[sched];
+  dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
+  const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
+  const bool two = kTwoStep<T, SB> && p->unroll[sched] == 2;
+  constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
+  auto launch = [&](auto kern) {
+    if (p->ev_start) cudaEventRecord(p->ev_start, st);
+    kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch, ro);
+    if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
+  };
+  if (RES || op == CTGB_OP_PROJECTION) {
+    if (two) launch(k_det_gather<T, SB, kA, U2, RES>);
+    else launch(k_det_gather<T, SB, kA, 3, RES>);
+  } else {
+    if (two) launch(k_det_gather<T, SB, kBt, U2>);
+    else launch(k_det_gather<T, SB, kBt, 3>);
+  }
+  return CTGB_OK;
+}
+
+// Staged image gather (A^T, B, fbp's backprojection, single-view B) from the
+// sinogram planes qb; unless `planes_ready`, qb is first filled from x (re-layout,
+// or the ramp filter for fbp).
+template <class T, int SB>
+static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, const T* x, T* y, int batch,
+                      T* qb, bool planes_ready, cudaStream_t st) {
+  const int G = (batch + SB - 1) / SB;
+  const HostGeom& g = p->geom;
+  if (!planes_ready && op == CTGB_OP_FBP) {
+    const size_t smem = ((size_t)4 * g.D + (size_t)SB * g.D) * sizeof(T);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_ramp_filter<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ramp filter smem: ") + cudaGetErrorString(e));
+    }
+    k_ramp_filter<T, SB><<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
+  } else if (!planes_ready) {
+    const size_t n = (size_t)G * g.V * P.Dp;
     const int tb = 256;
     const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
     PrefetchList pf{};
-    const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
-    pf.ptr[0] = P.lg; pf.bytes[0] = VL * 4 * sizeof(T);
-    pf.ptr[1] = P.ls; pf.bytes[1] = VL * sizeof(T);
-    pf.ptr[2] = P.db2; pf.bytes[2] = (VD + g.V) * 2 * sizeof(T);
-    pf.ptr[3] = P.wd; pf.bytes[3] = VD * sizeof(T);
-    pf.ptr[4] = op == CTGB_OP_PROJECTION ? P.fq : P.fbt; pf.bytes[4] = VD * sizeof(T);
-    pf.n = 5;
-    k_layout_image<T, SB><<<nb, tb, 0, st>>>(x, imx, imy, batch, g.H, g.W, G, pf);
-    const int wpc = p->warps[op];
-    dim3 grid((g.D + 31) / 32, (g.V + wpc - 1) / wpc, G);
-    const size_t acc_smem = (size_t)2 * SB * 32 * wpc * sizeof(T);
-    const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
-    auto launch = [&](auto kern) {
-      if (p->ev_start) cudaEventRecord(p->ev_start, st);
-      kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch);
-      if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
-    };
-    if (op == CTGB_OP_PROJECTION) {
-      if (two) launch(k_det_gather<T, SB, kA, kTwoStep<T, SB> ? 2 : 3>);
-      else launch(k_det_gather<T, SB, kA, 3>);
-    } else {
-      if (two) launch(k_det_gather<T, SB, kBt, kTwoStep<T, SB> ? 2 : 3>);
-      else launch(k_det_gather<T, SB, kBt, 3>);
-    }
-  } else {
-    T* qb = static_cast<T*>(ws);
-    if (op == CTGB_OP_FBP) {
-      const size_t smem = ((size_t)4 * g.D + (size_t)SB * g.D) * sizeof(T);
-      if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_ramp_filter<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ramp filter smem: ") + cudaGetErrorString(e));
-      }
-      k_ramp_filter<T, SB><<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
-    } else {
-      const size_t n = (size_t)G * g.V * P.Dp;
-      const int tb = 256;
-      const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
-      PrefetchList pf{};
-      const size_t VL = (size_t)g.V * g.L;
-      pf.ptr[0] = P.lp; pf.bytes[0] = VL * 4 * sizeof(T);
-      pf.ptr[1] = P.rec; pf.bytes[1] = (size_t)g.V * P.Dp * 4 * sizeof(T);
-      pf.ptr[2] = P.db2; pf.bytes[2] = ((size_t)g.V * g.D + g.V) * 2 * sizeof(T);
-      pf.n = 3;
-      k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr,
-                                             batch, g.V, g.D, P.Dp, G, pf);
-    }
-    const int wpc = p->warps[op];  // consumer warps (one pixel row each) + one producer warp
-    dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
-    const int nt = 32 * (wpc + 1);
-    const size_t smem = (size_t)2 * SB * nt * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
-    auto launch = [&](auto kern, T mul, T div) -> int {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
-      const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? 1 : view_split(g.V);
-      if (nsplit > 1) {
-        e = cudaMemsetAsync(y, 0, (size_t)batch * g.H * g.W * sizeof(T), st);
-        if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather clear: ") + cudaGetErrorString(e));
-      }
-      if (p->ev_start) cudaEventRecord(p->ev_start, st);
-      kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, batch, mul, div, nsplit);
-      if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
-      return CTGB_OK;
-    };
-    constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
-    const bool two = kTwoStep<T, SB> && p->unroll[op] == 2;
-    int rc;
-    if (op == CTGB_OP_BACKPROJECTION_SV)
-      rc = two ? launch(k_pix_gather<T, SB, kB, U2, true>, T(1), T(1))
-               : launch(k_pix_gather<T, SB, kB, 3, true>, T(1), T(1));
-    else if (op == CTGB_OP_PROJECTION_T)
-      rc = two ? launch(k_pix_gather<T, SB, kAt, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kAt, 3>, T(1), T(1));
-    else if (op == CTGB_OP_BACKPROJECTION)
-      rc = two ? launch(k_pix_gather<T, SB, kB, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kB, 3>, T(1), T(1));
-    else
-      rc = two ? launch(k_pix_gather<T, SB, kB, U2>, P.dAng, T(2)) : launch(k_pix_gather<T, SB, kB, 3>, P.dAng, T(2));
-    if (rc != CTGB_OK) return rc;
+    const size_t VL = (size_t)g.V * g.L;
+    pf.ptr[0] = P.lp; pf.bytes[0] = VL * 4 * sizeof(T);
+    pf.ptr[1] = P.rec; pf.bytes[1] = (size_t)g.V * P.Dp * 4 * sizeof(T);
+    pf.ptr[2] = P.db2; pf.bytes[2] = ((size_t)g.V * g.D + g.V) * 2 * sizeof(T);
+    pf.n = 3;
+    k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr, batch,
+                                           g.V, g.D, P.Dp, G, pf);
   }
+  const int wpc = p->warps[sched];  // consumer warps (one pixel row each) + one producer warp
+  dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
+  const int nt = 32 * (wpc + 1);
+  const size_t smem = (size_t)2 * SB * nt * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
+  auto launch = [&](auto kern, T mul, T div) -> int {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
+    const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? 1 : view_split(g.V);
+    if (nsplit > 1) {
+      e = cudaMemsetAsync(y, 0, (size_t)batch * g.H * g.W * sizeof(T), st);
+      if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather clear: ") + cudaGetErrorString(e));
+    }
+    if (p->ev_start) cudaEventRecord(p->ev_start, st);
+    kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, batch, mul, div, nsplit);
+    if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
+    return CTGB_OK;
+  };
+  constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
+  const bool two = kTwoStep<T, SB> && p->unroll[sched] == 2;
+  if (op == CTGB_OP_BACKPROJECTION_SV)
+    return two ? launch(k_pix_gather<T, SB, kB, U2, true>, T(1), T(1))
+               : launch(k_pix_gather<T, SB, kB, 3, true>, T(1), T(1));
+  if (op == CTGB_OP_PROJECTION_T)
+    return two ? launch(k_pix_gather<T, SB, kAt, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kAt, 3>, T(1), T(1));
+  if (op == CTGB_OP_BACKPROJECTION)
+    return two ? launch(k_pix_gather<T, SB, kB, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kB, 3>, T(1), T(1));
+  return two ? launch(k_pix_gather<T, SB, kB, U2>, P.dAng, T(2)) : launch(k_pix_gather<T, SB, kB, 3>, P.dAng, T(2));
+}
+
+template <class T, int SB>
+static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* in, void* out, int batch,
+                  void* ws, cudaStream_t st) {
+  const T* x = static_cast<const T*>(in);
+  T* y = static_cast<T*>(out);
+  int rc;
+  if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
+    rc = launch_det<T, SB, false>(p, P, op, op, x, y, batch, ws, st);
+  else
+    rc = launch_pix<T, SB>(p, P, op, op, x, y, batch, static_cast<T*>(ws), false, st);
+  if (rc != CTGB_OK) return rc;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return CTGB_OK;
+}
+
+// Data-term gradient A^T(Ax - y): image re-layout, detector gather writing the
+// residual straight into the image gather's planes (and optionally to `res`),
+// image gather. The workspace holds both plane sets; the detector gather uses
+// projection's schedule, the image gather projection_t's.
+template <class T, int SB>
+static int run_gradient(const ctgb_plan* p, const DevPlan<T>& P, const T* x, const T* y, T* res, T* grad, int batch,
+                        void* ws, cudaStream_t st) {
+  const size_t G = (size_t)((batch + SB - 1) / SB);
+  T* qb = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + det_planes_bytes(p->geom, G, SB, sizeof(T)));
+  int rc = launch_det<T, SB, true>(p, P, CTGB_OP_PROJECTION, CTGB_OP_PROJECTION, x, nullptr, batch, ws, st,
+                                   ResidualOut<T>{y, res, qb});
+  if (rc == CTGB_OK)
+    rc = launch_pix<T, SB>(p, P, CTGB_OP_PROJECTION_T, CTGB_OP_PROJECTION_T, nullptr, grad, batch, qb, true, st);
+  if (rc != CTGB_OK) return rc;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   return CTGB_OK;
@@ -1400,6 +1494,48 @@ static int dispatch(const ctgb_plan* p, int op, const void* in, void* out, int b
       case 1: rc = run_op<double, 1>(p, p->pd, op, in, out, batch, ws, st); break;
       case 2: rc = run_op<double, 2>(p, p->pd, op, in, out, batch, ws, st); break;
       default: rc = run_op<double, 4>(p, p->pd, op, in, out, batch, ws, st); break;
+    }
+  }
+  if (cur != p->device && cur >= 0) cudaSetDevice(cur);
+  return rc;
+}
+
+static int dispatch_gradient(const ctgb_plan* p, const void* image, const void* sino, void* res, void* grad,
+                             int batch, void* ws, size_t wsb, void* stream) {
+  if (!p) return fail(CTGB_ERR_INVALID, "null plan");
+  if (batch < 0) return fail(CTGB_ERR_INVALID, "negative batch");
+  if (batch == 0) return CTGB_OK;
+  if (!image || !sino || !grad) return fail(CTGB_ERR_INVALID, "null image, sinogram or gradient pointer");
+  const size_t need = gradient_workspace_bytes(p, batch);
+  if (!ws || wsb < need) return fail(CTGB_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
+  if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) return fail(CTGB_ERR_INVALID, "workspace must be 256-byte aligned");
+  int cur = -1;
+  CTGB_CUDA(cudaGetDevice(&cur));
+  if (cur != p->device) CTGB_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int sb = gradient_sb(p, batch);
+  int rc;
+  if (p->dtype == 0) {
+    const float* x = static_cast<const float*>(image);
+    const float* y = static_cast<const float*>(sino);
+    float* r = static_cast<float*>(res);
+    float* gr = static_cast<float*>(grad);
+    switch (sb) {
+      case 1: rc = run_gradient<float, 1>(p, p->pf, x, y, r, gr, batch, ws, st); break;
+      case 2: rc = run_gradient<float, 2>(p, p->pf, x, y, r, gr, batch, ws, st); break;
+      case 4: rc = run_gradient<float, 4>(p, p->pf, x, y, r, gr, batch, ws, st); break;
+      case 8: rc = run_gradient<float, 8>(p, p->pf, x, y, r, gr, batch, ws, st); break;
+      default: rc = run_gradient<float, 16>(p, p->pf, x, y, r, gr, batch, ws, st); break;
+    }
+  } else {
+    const double* x = static_cast<const double*>(image);
+    const double* y = static_cast<const double*>(sino);
+    double* r = static_cast<double*>(res);
+    double* gr = static_cast<double*>(grad);
+    switch (sb) {
+      case 1: rc = run_gradient<double, 1>(p, p->pd, x, y, r, gr, batch, ws, st); break;
+      case 2: rc = run_gradient<double, 2>(p, p->pd, x, y, r, gr, batch, ws, st); break;
+      default: rc = run_gradient<double, 4>(p, p->pd, x, y, r, gr, batch, ws, st); break;
     }
   }
   if (cur != p->device && cur >= 0) cudaSetDevice(cur);
@@ -1820,7 +1956,8 @@ int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps) {
 }
 
 size_t ctgb_workspace_size(const ctgb_plan* plan, int op, int batch) {
-  if (!plan || batch <= 0 || op < 0 || op > 5) return 0;
+  if (!plan || batch <= 0 || op < 0 || op > 6) return 0;
+  if (op == CTGB_OP_DATA_GRADIENT) return ctgb::gradient_workspace_bytes(plan, batch);
   return ctgb::workspace_bytes(plan, op, batch);
 }
 
@@ -1846,6 +1983,10 @@ int ctgb_fbp(const ctgb_plan* p, const void* sino, void* image, int batch, void*
 int ctgb_backprojection_sv(const ctgb_plan* p, const void* sino, void* images, int batch, void* ws, size_t wsb,
                            void* stream) {
   return ctgb::dispatch(p, CTGB_OP_BACKPROJECTION_SV, sino, images, batch, ws, wsb, stream);
+}
+int ctgb_data_gradient(const ctgb_plan* p, const void* image, const void* sino, void* residual, void* grad, int batch,
+                       void* ws, size_t wsb, void* stream) {
+  return ctgb::dispatch_gradient(p, image, sino, residual, grad, batch, ws, wsb, stream);
 }
 
 int ctgb_projection_noalloc(const ctgb_plan* p, const void* image, void* sino, int batch, void* stream) {

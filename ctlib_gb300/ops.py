@@ -216,3 +216,38 @@ def backprojection_sv(projection: torch.Tensor, options) -> torch.Tensor:
     B x 1 x V x D -> B x V x H x W, image v holding view v's term of
     backprojection (src/ctlib.cpp:45-54, src/fan_ed_kernel.cu:946-1161)."""
     return _apply(N.OP_BACKPROJECTION_SV, projection, options, "projection")
+
+
+def data_gradient(image: torch.Tensor, projection: torch.Tensor, options, return_residual: bool = False):
+    """Gradient of the data term 0.5*||A x - y||^2: A^T(A x - y) for an image
+    B x 1 x H x W and a measured sinogram B x 1 x V x D (ctgb_data_gradient).
+    The same values as ``projection_t(projection(x) - y)``, without the separate
+    subtraction and sinogram re-layout. With ``return_residual`` also returns
+    A x - y. No single counterpart in the reference, which composes it from
+    projection and projection_t (src/ctlib.cpp:56-84)."""
+    import ctypes
+    x = _check_input(image, "image")
+    y = _check_input(projection, "projection")
+    if y.dtype != x.dtype or y.device != x.device:
+        raise ValueError("image and projection must share dtype and device")
+    plan = get_plan(options, x.dtype, x.device)
+    B = x.shape[0]
+    if tuple(x.shape[2:]) != (plan.height, plan.width):
+        raise ValueError(f"image is {tuple(x.shape[2:])}, options give height x width {(plan.height, plan.width)}")
+    if tuple(y.shape) != (B, 1, plan.views, plan.dets):
+        raise ValueError(f"projection is {tuple(y.shape)}, expected {(B, 1, plan.views, plan.dets)}")
+    grad = torch.empty_like(x)
+    res = torch.empty_like(y) if return_residual else None
+    if B > 0:
+        # the two kernels run with the schedules of projection and projection_t
+        tune.apply_cached(plan, N.OP_PROJECTION, B)
+        tune.apply_cached(plan, N.OP_PROJECTION_T, B)
+        nbytes = plan.workspace_bytes(N.OP_DATA_GRADIENT, B)
+        with torch.cuda.device(x.device):
+            ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+            stream = torch.cuda.current_stream(x.device)
+            rc = N.lib().ctgb_data_gradient(plan.handle, x.data_ptr(), y.data_ptr(),
+                                            res.data_ptr() if res is not None else None, grad.data_ptr(), B,
+                                            ws.data_ptr(), ctypes.c_size_t(nbytes), stream.cuda_stream)
+        N.check(rc, "data_gradient")
+    return (grad, res) if return_residual else grad

@@ -43,7 +43,8 @@ enum {
   CTGB_OP_BACKPROJECTION = 2,
   CTGB_OP_BACKPROJECTION_T = 3,
   CTGB_OP_FBP = 4,
-  CTGB_OP_BACKPROJECTION_SV = 5
+  CTGB_OP_BACKPROJECTION_SV = 5,
+  CTGB_OP_DATA_GRADIENT = 6 /* for ctgb_workspace_size only */
 };
 
 /* Decode an options vector (host array, the reference's layout: fan
@@ -130,6 +131,20 @@ int ctgb_fbp(const ctgb_plan* plan, const void* sino, void* image, int batch, vo
  * CTGB_OP_BACKPROJECTION_SV in ctgb_workspace_size. */
 int ctgb_backprojection_sv(const ctgb_plan* plan, const void* sino, void* images, int batch, void* workspace,
                            size_t workspace_bytes, void* stream);
+
+/* Gradient of the data term 0.5*||A x - y||^2 for iterative reconstruction:
+ * grad = A^T (A x - y), image B x 1 x H x W and measured sinogram y
+ * B x 1 x V x D in, grad B x 1 x H x W out; `residual` (B x 1 x V x D, may be
+ * NULL) receives A x - y, from which the caller forms the loss. The same values
+ * as projection, a subtraction and projection_t, without a separate subtraction
+ * or sinogram re-layout: the projection kernel writes the residual straight into
+ * the backprojection's input planes. Uses the schedules set for
+ * CTGB_OP_PROJECTION (its first kernel) and CTGB_OP_PROJECTION_T (its second);
+ * workspace: ctgb_workspace_size(plan, CTGB_OP_DATA_GRADIENT, batch). No single
+ * counterpart in the reference: a caller composes it from projection and
+ * projection_t (src/ctlib.cpp:56-84). */
+int ctgb_data_gradient(const ctgb_plan* plan, const void* image, const void* sino, void* residual, void* grad,
+                       int batch, void* workspace, size_t workspace_bytes, void* stream);
 
 /* A (as ctgb_projection) for callers that cannot allocate device memory.
  * No counterpart in the reference. Some callers of these operators may not
