@@ -317,6 +317,26 @@ def run_ours(args):
         e2e_mean = float(t.item())
     e2e_value = ws * ru_step / (e2e_mean / 1e3)
 
+    # -- data-term gradient A^T(Ax - y): fused call vs composed operators -----
+    from ctlib_gb300.ops import data_gradient
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    grad_fused = timed(lambda: data_gradient(img, y_meas, opts))
+    grad_composed = timed(lambda: ctlib.projection_t(ctlib.projection(img, opts) - y_meas, opts))
+
     # -- parity of the timed operator pair vs the FP64 oracle (1 slice) -------
     parity = None
     if rank == 0:
@@ -373,6 +393,9 @@ def run_ours(args):
                         "h2d_bytes_per_step": int(img_h.numel() * 4),
                         "d2h_bytes_per_step": int(img_h.numel() * 4 + 4),
                         "path": "ctlib_gb300.autograd.Projector: H2D image, A, loss, backward (A^T), D2H grad+loss"},
+                "data_gradient": {"ms_fused": grad_fused, "ms_composed": grad_composed,
+                                  "note": "A^T(Ax - y) for the same batch: ctgb_data_gradient vs projection, "
+                                          "subtraction, projection_t"},
                 "gpu_launches": 4 * args.steps,
                 "clocks": clocks, "roofline": roof, "roofline_fp32": roof_fp32, "parity": parity,
                 "cpu_baseline": cb}
