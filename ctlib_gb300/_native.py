@@ -78,6 +78,8 @@ def _declare(l):
     l.ctgb_plan_set_schedule.restype = c_int
     l.ctgb_plan_set_unroll.argtypes = [vp, c_int, c_int]
     l.ctgb_plan_set_unroll.restype = c_int
+    l.ctgb_plan_set_filter.argtypes = [vp, c_int, c_int]
+    l.ctgb_plan_set_filter.restype = c_int
     l.ctgb_plan_set_kernel_events.argtypes = [vp, vp, vp]
     l.ctgb_plan_set_kernel_events.restype = c_int
     l.ctgb_workspace_size.argtypes = [vp, c_int, c_int]
@@ -140,7 +142,7 @@ def check(rc: int, what: str):
     raise RuntimeError(msg)
 
 
-EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_plan_set_schedule", "ctgb_plan_set_unroll",
+EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_plan_set_schedule", "ctgb_plan_set_unroll", "ctgb_plan_set_filter",
             "ctgb_plan_set_kernel_events",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",

@@ -73,6 +73,7 @@ template <class T>
 struct DevPlan {
   int V, D, W, H, L, scan;
   int Dp;             // D rounded up to a multiple of 4: row stride of cell records and sinogram planes
+  int even_taps;      // fbp filter with non-zero even offsets (windowed kernels), besides the centre
   T dImg, s2r, dAng, wscale;
   const int* flags;   // V
   const T* src;       // V*2   source x, y
@@ -1107,49 +1108,55 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     // far, small taps must not be added straight onto the large running sum;
     // the low parts of the taps go to their own plain sum (plo)
     T acc[8], comp[8], part[8], plo[8];
-    T win[8], wlo[8];
-    // window: win[i] = h(m - k0 - 2i) for the current input m (opposite parity)
-    int m = 1 - par;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       acc[i] = T(0);
       comp[i] = T(0);
       part[i] = T(0);
       plo[i] = T(0);
-      const int off = m - k0 - 2 * i;  // odd
-      const int ti = off + D - 1;
-      const bool ok = ti >= 0 && ti < 2 * D - 1;
-      win[i] = ok ? taps[ti] : T(0);
-      wlo[i] = ok ? tapl[ti] : T(0);
     }
-    for (int step = 0; m < D; m += 2, ++step) {
-      const T xm = row[m];
+    int step = 0;
+    // one pass over the inputs m = m0, m0+2, ...: window win[i] = h(m - k0 - 2i)
+    auto pass = [&](int m0) {
+      T win[8], wlo[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) part[i] = fma(xm, win[i], part[i]);
-      if constexpr (kLo) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) plo[i] = fma(xm, wlo[i], plo[i]);
+      for (int i = 0; i < 8; ++i) {
+        const int ti = m0 - k0 - 2 * i + D - 1;
+        const bool ok = ti >= 0 && ti < 2 * D - 1;
+        win[i] = ok ? taps[ti] : T(0);
+        wlo[i] = ok ? tapl[ti] : T(0);
       }
+      for (int m = m0; m < D; m += 2, ++step) {
+        const T xm = row[m];
 #pragma unroll
-      for (int i = 7; i > 0; --i) {
-        win[i] = win[i - 1];
-        wlo[i] = wlo[i - 1];
-      }
-      const int ti = m + 2 - k0 + D - 1;
-      const bool ok = ti >= 0 && ti < 2 * D - 1;
-      win[0] = ok ? taps[ti] : T(0);
-      wlo[0] = ok ? tapl[ti] : T(0);
-      if ((step & 15) == 15) {
+        for (int i = 0; i < 8; ++i) part[i] = fma(xm, win[i], part[i]);
+        if constexpr (kLo) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const T y = sub_rn(part[i], comp[i]);
-          const T t = add_rn(acc[i], y);
-          comp[i] = sub_rn(sub_rn(t, acc[i]), y);
-          acc[i] = t;
-          part[i] = T(0);
+          for (int i = 0; i < 8; ++i) plo[i] = fma(xm, wlo[i], plo[i]);
+        }
+#pragma unroll
+        for (int i = 7; i > 0; --i) {
+          win[i] = win[i - 1];
+          wlo[i] = wlo[i - 1];
+        }
+        const int ti = m + 2 - k0 + D - 1;
+        const bool ok = ti >= 0 && ti < 2 * D - 1;
+        win[0] = ok ? taps[ti] : T(0);
+        wlo[0] = ok ? tapl[ti] : T(0);
+        if ((step & 15) == 15) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const T y = sub_rn(part[i], comp[i]);
+            const T t = add_rn(acc[i], y);
+            comp[i] = sub_rn(sub_rn(t, acc[i]), y);
+            acc[i] = t;
+            part[i] = T(0);
+          }
         }
       }
-    }
+    };
+    pass(1 - par);                // odd offsets: the only non-zero ones of the RL kernel besides 0
+    if (P.even_taps) pass(par);   // windowed kernels: even offsets, the centre tap included
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[i] = add_rn(acc[i], sub_rn(part[i], comp[i]));
     const T h0 = taps[D - 1], h0l = tapl[D - 1];
@@ -1157,8 +1164,14 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     for (int i = 0; i < 8; ++i) {
       const int k = k0 + 2 * i;
       if (k < D) {
-        T val = fma(h0, row[k], acc[i]);
-        if constexpr (kLo) val = add_rn(val, fma(h0l, row[k], plo[i]));
+        T val;
+        if (P.even_taps) {
+          val = acc[i];
+          if constexpr (kLo) val = add_rn(val, plo[i]);
+        } else {
+          val = fma(h0, row[k], acc[i]);
+          if constexpr (kLo) val = add_rn(val, fma(h0l, row[k], plo[i]));
+        }
         const int di = flip ? D - 1 - k : k;
         qv[((size_t)(s / Planes<SB>::QW) * qs + di) * Planes<SB>::QW + (s % Planes<SB>::QW)] = val;
       }
@@ -1944,6 +1957,40 @@ int ctgb_plan_set_kernel_events(ctgb_plan* plan, void* start_event, void* stop_e
     return ctgb::fail(CTGB_ERR_INVALID, "give both events or neither");
   plan->ev_start = static_cast<cudaEvent_t>(start_event);
   plan->ev_stop = static_cast<cudaEvent_t>(stop_event);
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_filter(ctgb_plan* plan, int window, int ea_exact) {
+  using namespace ctgb;
+  if (!plan) return fail(CTGB_ERR_INVALID, "null plan");
+  HostGeom g2 = plan->geom;
+  std::string err;
+  if (!filter_taps(g2, window, ea_exact != 0, err)) return fail(CTGB_ERR_INVALID, err);
+  int cur = -1;
+  CTGB_CUDA(cudaGetDevice(&cur));
+  if (cur != plan->device) CTGB_CUDA(cudaSetDevice(plan->device));
+  // kernels of this plan still in flight may be reading the taps
+  cudaError_t e = cudaDeviceSynchronize();
+  const size_t n = g2.taps.size();
+  if (e == cudaSuccess) {
+    if (plan->dtype == 0) {
+      std::vector<float> hi(n), lo(n);
+      for (size_t i = 0; i < n; ++i) { hi[i] = (float)g2.taps[i]; lo[i] = (float)g2.taps_lo[i]; }
+      e = cudaMemcpy(const_cast<float*>(plan->pf.taps), hi.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(const_cast<float*>(plan->pf.tapl), lo.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    } else {
+      e = cudaMemcpy(const_cast<double*>(plan->pd.taps), g2.taps.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(const_cast<double*>(plan->pd.tapl), g2.taps_lo.data(), n * sizeof(double),
+                       cudaMemcpyHostToDevice);
+    }
+  }
+  if (cur != plan->device && cur >= 0) cudaSetDevice(cur);
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("filter taps: ") + cudaGetErrorString(e));
+  plan->geom.taps = g2.taps;
+  plan->geom.taps_lo = g2.taps_lo;
+  plan->pf.even_taps = plan->pd.even_taps = window != kRamLak;
   return CTGB_OK;
 }
 

@@ -194,6 +194,7 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
   // the remainder to the fp64 taps: the RL kernel's response nearly cancels on
   // smooth rows, so the fp32 rounding of the taps alone moves an equal-angle
   // reconstruction by ~1e-5 relative.
+  g.dfilt = (double)dfilt;
   g.taps.assign(2 * D - 1, 0.0);
   g.taps_lo.assign(2 * D - 1, 0.0);
   const double df = (double)dfilt;
@@ -214,9 +215,61 @@ bool build(const double* o, int n, HostGeom& g, std::string& err) {
 
 }  // namespace
 
+// RL kernel value at integer offset x for tap spacing d (src/fan_ed_kernel.cu:926-943)
+static double rl_tap(long x, double d) {
+  const double PI = std::acos(-1.0);
+  if (x == 0) return 1 / (4 * d * d);
+  if (std::labs(x) % 2 == 1) return -1 / (PI * PI * (double)x * (double)x * d * d);
+  return 0.0;
+}
+
+bool filter_taps(HostGeom& g, int window, bool ea_exact, std::string& err) {
+  if (window < kRamLak || window > kHann) {
+    err = "filter window must be 0 (Ram-Lak), 1 (Shepp-Logan) or 2 (Hann)";
+    return false;
+  }
+  if (ea_exact && g.scan != kFanEA) {
+    err = "the exact equal-angle kernel applies to equal-angle fan beams (scan_type 1) only";
+    return false;
+  }
+  const int D = g.D;
+  const double d = g.dfilt;
+  if (window == kRamLak && !ea_exact) {  // the reference's taps, as built with the plan
+    HostGeom fresh;
+    std::string e;
+    if (!build_geometry(g.options.data(), (int)g.options.size(), g.dtype, fresh, e)) {
+      err = e;
+      return false;
+    }
+    g.taps = fresh.taps;
+    g.taps_lo = fresh.taps_lo;
+    return true;
+  }
+  const double PI = std::acos(-1.0);
+  g.taps.assign(2 * D - 1, 0.0);
+  g.taps_lo.assign(2 * D - 1, 0.0);
+  for (int j = 0; j < 2 * D - 1; ++j) {
+    const long x = j - D + 1;
+    double h;
+    if (window == kSheppLogan) h = -2 / (PI * PI * d * d * (4.0 * (double)x * (double)x - 1.0));
+    else if (window == kHann) h = 0.25 * rl_tap(x - 1, d) + 0.5 * rl_tap(x, d) + 0.25 * rl_tap(x + 1, d);
+    else h = rl_tap(x, d);
+    if (ea_exact && x != 0) {
+      const double gam = (double)x * d;
+      const double f = gam / std::sin(gam);
+      h *= f * f;
+    }
+    const double hi = g.dtype == 0 ? (double)(float)h : h;
+    g.taps[j] = hi;
+    g.taps_lo[j] = g.dtype == 0 ? h - hi : 0.0;
+  }
+  return true;
+}
+
 bool build_geometry(const double* options, int n_options, int dtype, HostGeom& g, std::string& err) {
   g = HostGeom();
   g.dtype = dtype;
+  if (options && n_options > 0) g.options.assign(options, options + n_options);
   if (dtype == 0) return build<float>(options, n_options, g, err);
   if (dtype == 1) return build<double>(options, n_options, g, err);
   err = "dtype must be 0 (float32) or 1 (float64)";

@@ -41,11 +41,24 @@ struct HostGeom {
   double wscale = 1.0;
   std::vector<double> taps;    // 2D-1: RL ramp taps (src/fan_ed_kernel.cu:926-943)
   std::vector<double> taps_lo; // 2D-1: fp64 tap minus the stored one (fp32 plans), else 0
+  double dfilt = 0.0;          // tap spacing of the ramp filter (virtual bin, or dDet)
+  std::vector<double> options; // the options vector the geometry was built from
   double x0 = 0, y0 = 0;       // left image edge x, bottom image edge y
 };
 
 // Parse the reference's options vector and build the geometry. dtype 0 = fp32,
 // 1 = fp64. Returns false and sets `err` on invalid options.
 bool build_geometry(const double* options, int n_options, int dtype, HostGeom& g, std::string& err);
+
+// fbp filter windows: the reference's Ram-Lak (RL) kernel, Shepp-Logan, and RL
+// under a Hann window (its exact discrete form, [1/4, 1/2, 1/4] * RL).
+enum FilterWindow { kRamLak = 0, kSheppLogan = 1, kHann = 2 };
+
+// Ramp filter taps (2D-1, offsets -(D-1)..D-1) of `window` into g.taps /
+// g.taps_lo, for the plan's dtype. ea_exact (equal-angle fans only) multiplies
+// each tap by (n dDet / sin(n dDet))^2, the factor that makes the RL kernel
+// exact on equiangular samples. RamLak without ea_exact reproduces the
+// reference's taps; the others have no counterpart in it.
+bool filter_taps(HostGeom& g, int window, bool ea_exact, std::string& err);
 
 }  // namespace ctgb

@@ -118,18 +118,25 @@ def _option_values(options) -> tuple:
     return tuple(float(v) for v in options)
 
 
-def get_plan(options, dtype: torch.dtype, device) -> Plan:
-    """Cached plan for (options values, dtype, device)."""
+FILTERS = {"ram-lak": 0, "shepp-logan": 1, "hann": 2}
+
+
+def get_plan(options, dtype: torch.dtype, device, filt: tuple = (0, 0)) -> Plan:
+    """Cached plan for (options values, dtype, device, fbp filter). ``filt`` is
+    (window, ea_exact) as for ctgb_plan_set_filter; (0, 0) is the reference's
+    Ram-Lak filter."""
     dev = torch.device(device)
     idx = dev.index if dev.index is not None else torch.cuda.current_device()
     vals = _option_values(options)
-    key = (vals, dtype, idx)
+    key = (vals, dtype, idx, tuple(filt))
     with _plan_lock:
         p = _plans.get(key)
         if p is not None:
             _plans.move_to_end(key)
             return p
     p = Plan(vals, dtype, idx)
+    if tuple(filt) != (0, 0):
+        N.check(N.lib().ctgb_plan_set_filter(p.handle, int(filt[0]), int(filt[1])), "filter")
     with _plan_lock:
         _plans[key] = p
         while len(_plans) > _MAX_PLANS:
@@ -159,9 +166,9 @@ def _check_input(x: torch.Tensor, name: str) -> torch.Tensor:
     return x
 
 
-def _apply(op: int, x: torch.Tensor, options, name: str) -> torch.Tensor:
+def _apply(op: int, x: torch.Tensor, options, name: str, filt: tuple = (0, 0)) -> torch.Tensor:
     x = _check_input(x, name)
-    plan = get_plan(options, x.dtype, x.device)
+    plan = get_plan(options, x.dtype, x.device, filt)
     B = x.shape[0]
     img_shape = (plan.height, plan.width)
     sino_shape = (plan.views, plan.dets)
@@ -206,9 +213,18 @@ def backprojection_t(image: torch.Tensor, options) -> torch.Tensor:
     return _apply(N.OP_BACKPROJECTION_T, image, options, "image")
 
 
-def fbp(projection: torch.Tensor, options) -> torch.Tensor:
-    """RL-filtered backprojection: sinogram -> image (src/ctlib.cpp:86-99)."""
-    return _apply(N.OP_FBP, projection, options, "projection")
+def fbp(projection: torch.Tensor, options, filter: str = "ram-lak", ea_exact: bool = False) -> torch.Tensor:
+    """Filtered backprojection: sinogram -> image (src/ctlib.cpp:86-99).
+
+    The defaults reproduce the reference: the Ram-Lak kernel with the
+    reference's detector pre-weights. ``filter`` may also be "shepp-logan" or
+    "hann" (Ram-Lak under a Hann window); ``ea_exact`` (equal-angle fans only)
+    uses the kernel that is exact on equiangular samples, (g/sin g)^2 times
+    Ram-Lak, where the reference applies the parallel-beam kernel in angle
+    units. Neither option exists in the reference."""
+    if filter not in FILTERS:
+        raise ValueError(f"filter must be one of {sorted(FILTERS)}, got {filter!r}")
+    return _apply(N.OP_FBP, projection, options, "projection", (FILTERS[filter], int(bool(ea_exact))))
 
 
 def backprojection_sv(projection: torch.Tensor, options) -> torch.Tensor:

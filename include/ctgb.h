@@ -77,6 +77,16 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
  * in the reference (its merge walk has no fixed step count). */
 int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps);
 
+/* Ramp filter of fbp on this plan: window 0 = Ram-Lak (the reference's kernel,
+ * the default), 1 = Shepp-Logan, 2 = Ram-Lak under a Hann window; ea_exact != 0
+ * (equal-angle fans only) scales each tap by (n dDet / sin(n dDet))^2, which
+ * makes the kernel exact on equiangular samples where the reference applies the
+ * parallel-beam kernel in angle units (src/fan_ea_kernel.cu:1074-1093).
+ * Synchronises the plan's device and rewrites the plan's taps; a ragged batch
+ * uses the filters its plans had when it was created. Only (0, 0) has a
+ * counterpart in the reference (rlfilter, src/fan_ed_kernel.cu:926-943). */
+int ctgb_plan_set_filter(ctgb_plan* plan, int window, int ea_exact);
+
 /* Measurement hook: when both are non-null, every later operator call on this
  * plan records `start_event` right before its gather kernel and `stop_event`
  * right after it, on the call's stream (cudaEvent_t handles created with

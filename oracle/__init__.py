@@ -37,6 +37,8 @@ def _load_oracle():
                                    ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_int]
         lib.oracle_run.restype = ctypes.c_int
+        lib.oracle_set_filter.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.oracle_set_filter.restype = ctypes.c_int
         lib.oracle_view_flags.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p]
         lib.oracle_max_threads.restype = ctypes.c_int
@@ -94,6 +96,22 @@ def run(op, x: np.ndarray, opts, mode: int = MODE_F64_ON_F32, threads: int = 0) 
     if rc != 0:
         raise ValueError(f"oracle_run failed with code {rc}")
     return out
+
+
+FILTERS = {"ram-lak": 0, "shepp-logan": 1, "hann": 2}
+
+
+def fbp(x: np.ndarray, opts, mode: int = MODE_F64_ON_F32, filter: str = "ram-lak", ea_exact: bool = False,
+        threads: int = 0) -> np.ndarray:
+    """fbp with a chosen filter window (and the exact equal-angle kernel);
+    the defaults are the reference's Ram-Lak filter."""
+    lib = _load_oracle()
+    if lib.oracle_set_filter(FILTERS[filter], int(bool(ea_exact))) != 0:
+        raise ValueError(filter)
+    try:
+        return run(OP_FBP, x, opts, mode, threads)
+    finally:
+        lib.oracle_set_filter(0, 0)
 
 
 def view_flags(opts, mode: int = MODE_F32):

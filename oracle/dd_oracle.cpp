@@ -356,6 +356,43 @@ void ramp_taps(int D, T d, T* h) {
   }
 }
 
+// fbp filter selected for the oracle's fbp (tests only): window 0 Ram-Lak (the
+// reference), 1 Shepp-Logan, 2 Ram-Lak under a Hann window; ea_exact scales the
+// taps by (n d / sin(n d))^2 (equal-angle fans). The variants restate published
+// kernels in fp64: Shepp & Logan (1974), h(n) = -2 / (pi^2 d^2 (4 n^2 - 1)); the
+// Hann window as its discrete convolution [1/4, 1/2, 1/4] with Ram-Lak; the
+// equiangular fan-beam kernel of Kak & Slaney (ch. 3), (gamma / sin gamma)^2
+// times the ramp kernel.
+static int g_window = 0, g_ea_exact = 0;
+
+static double rl_tap64(long x, double d) {
+  const double PI = std::acos(-1.0);
+  if (x == 0) return 1 / (4 * d * d);
+  if (std::labs(x) % 2 == 1) return -1 / (PI * PI * (double)x * (double)x * d * d);
+  return 0.0;
+}
+
+template <class T>
+void filter_taps(int D, T d, T* h) {
+  if (g_window == 0 && !g_ea_exact) {
+    ramp_taps(D, d, h);
+    return;
+  }
+  const double PI = std::acos(-1.0), dd = (double)d;
+  for (int j = 0; j < 2 * D - 1; ++j) {
+    const long x = j - D + 1;
+    double v;
+    if (g_window == 1) v = -2 / (PI * PI * dd * dd * (4.0 * (double)x * (double)x - 1.0));
+    else if (g_window == 2) v = 0.25 * rl_tap64(x - 1, dd) + 0.5 * rl_tap64(x, dd) + 0.25 * rl_tap64(x + 1, dd);
+    else v = rl_tap64(x, dd);
+    if (g_ea_exact && x != 0) {
+      const double gam = (double)x * dd;
+      v *= (gam / std::sin(gam)) * (gam / std::sin(gam));
+    }
+    h[j] = (T)v;
+  }
+}
+
 // FBP: detector pre-weight, RL filtering as a zero-padded linear convolution
 // along the detector axis (fp64 accumulation), backprojection, x dAng/2
 // (src/fan_ed_kernel.cu:1333-1382, src/fan_ea_kernel.cu:1059-1107,
@@ -387,7 +424,7 @@ void fbp(const Opts<T>& o, const std::vector<View<T>>& views, int B, const T* si
     dfilt = o.dDet;
   }
   std::vector<T> h(2 * D - 1);
-  ramp_taps(D, dfilt, h.data());
+  filter_taps(D, dfilt, h.data());
   std::vector<T> filt((size_t)B * V * D);
 #pragma omp parallel
   {
@@ -469,6 +506,14 @@ int oracle_run(int op, const double* opts, int nopts, int mode, int batch, const
     return run<double>(op, o32.data(), nopts, true, batch, in, out);
   }
   return 3;
+}
+
+// filter of the oracle's fbp (see filter_taps); returns 1 on a bad window
+int oracle_set_filter(int window, int ea_exact) {
+  if (window < 0 || window > 2) return 1;
+  g_window = window;
+  g_ea_exact = ea_exact != 0;
+  return 0;
 }
 
 // per-view branch (1 = image rows are the lines) and flip flags, for tests
