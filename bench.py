@@ -177,8 +177,75 @@ def run_reference(args):
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
+    rc = _reference_cuda(w, args)
+    if rc is not None:
+        line["reference_cuda"] = rc
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _reference_cuda(w, args):
+    """The reference's own CUDA kernels (src/fan_ed_kernel.cu prj_fan_ed and
+    prj_t_fan_ed, compiled unchanged for sm_103a, oracle/ref_cuda.py) on the full
+    workload: one step = projection then projection_t of the whole batch, each
+    call allocating its output as the reference's wrapper does, L2 flushed
+    before every step, CUDA events on the launching stream. None when there is
+    no GPU or the cubins were not built."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import ref_cuda
+        if not ref_cuda.available():
+            return None
+    except Exception:
+        return None
+    from ctlib_gb300.workloads import phantoms
+    ref = ref_cuda.get()
+    dev = ref.device
+    stream = torch.cuda.current_stream(dev)
+    opts = torch.tensor(w.slices[0].options, dtype=torch.float32, device=dev)
+    img_h = torch.from_numpy(np.stack(phantoms(w))[:, None]).contiguous()
+    img = img_h.to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(1, args.warmup)):
+        ref.run(1, ref.run(0, img, opts), opts)
+    torch.cuda.synchronize()
+    t_a, t_at = [], []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        s = ref.run(0, img, opts)
+        e1.record(stream)
+        ref.run(1, s, opts)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        t_a.append(e0.elapsed_time(e1))
+        t_at.append(e1.elapsed_time(e2))
+    ms = statistics.mean(a + b for a, b in zip(t_a, t_at))
+    ru = 2 * w.ray_updates()
+    # end to end: host image in, host image out, as a reference user would call it
+    img_pin = img_h.pin_memory()
+    out_h = torch.empty_like(img_h).pin_memory()
+    e2e = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        x = img_pin.to(dev, non_blocking=True)
+        out_h.copy_(ref.run(1, ref.run(0, x, opts), opts), non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e.append(a.elapsed_time(b))
+    e2e_ms = statistics.mean(e2e)
+    return {"value": ru / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "ms_projection": statistics.mean(t_a), "ms_projection_t": statistics.mean(t_at),
+            "e2e": {"value": ru / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": img_h.numel() * 4, "d2h_bytes_per_step": img_h.numel() * 4},
+            "kind": "reference CUDA kernels (src/fan_ed_kernel.cu) compiled for sm_103a, launched with the "
+                    "reference wrappers' grids and output allocations",
+            "dtype": "f32", "gpu_launches_per_step": 2}
 
 
 def _fp32_peak(device) -> dict:

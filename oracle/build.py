@@ -15,7 +15,18 @@
   harmless because all warps read before any writes, but which a one-thread-at-
   a-time execution would otherwise turn into a real read-after-write.
 
-Both use plain g++ (no cmake, no torch headers). The oracle is built with
+* ``build_ref_gpu()`` compiles the same three reference files for the GPU, as
+  the reference's ``CUDAExtension`` does but for sm_103a, into
+  ``oracle/_ref/ref_<file>.cubin.gz``, which ``ref_cuda.py`` loads through the
+  CUDA driver API. A generated wrapper (``oracle/_build/ref_gpu/*.cu``)
+  includes the reference file by name from the checkout (no copy), turns the
+  host wrappers' ``AT_DISPATCH_FLOATING_TYPES`` launches into nothing (they
+  need libtorch at run time) and instantiates every kernel for float and
+  double. It needs nvcc and the torch headers, so it runs only where a
+  checkout is present; the compressed cubins travel with the repository's
+  working tree to machines without one.
+
+``build_oracle`` and ``build_ref`` use plain g++ (no cmake, no torch headers). The oracle is built with
 ``-ffp-contract=off`` so it rounds identically on x86-64 and aarch64 (the fused
 operations it means are written as std::fma). The reference kernels are built
 with FMA contraction on, as nvcc compiles them by default (--fmad=true), so
@@ -111,6 +122,90 @@ def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | No
     return REF_SO
 
 
+# kernels of each reference file with the number of option pointers they take
+# (src/fan_ed_kernel.cu:24-946, src/fan_ea_kernel.cu:23-904,
+#  src/para_kernel.cu:8-666); rlfilter takes (filter, dets, dDet)
+REF_GPU_KERNELS = {
+    "ref_fan_ed": (("prj_fan_ed", "prj_t_fan_ed", "bprj_fan_ed", "bprj_t_fan_ed", "bprj_sv_fan_ed"), 11),
+    "ref_fan_ea": (("prj_fan_ea", "prj_t_fan_ea", "bprj_fan_ea", "bprj_t_fan_ea"), 11),
+    "ref_para": (("prj_para", "prj_t_para", "bprj_para", "bprj_t_para"), 9),
+}
+
+
+def ref_cubin_path(ns: str) -> str:
+    return os.path.join(REF_DIR, f"{ns}.cubin.gz")
+
+
+def _ref_gpu_wrapper(ns: str, fname: str) -> str:
+    kernels, nptr = REF_GPU_KERNELS[ns]
+    acc = "torch::PackedTensorAccessor<T, 4, torch::RestrictPtrTraits, size_t>"
+    lines = [
+        "// Written by oracle/build.py: the reference's kernels of " + fname + ",",
+        "// included by name from the checkout, instantiated for float and double.",
+        "// Test infrastructure only.",
+        "#include <torch/extension.h>",
+        "#undef AT_DISPATCH_FLOATING_TYPES",
+        "#define AT_DISPATCH_FLOATING_TYPES(TYPE, NAME, ...)",
+        f'#include "{fname}"',
+    ]
+    for t in ("float", "double"):
+        a = acc.replace("<T,", f"<{t},")
+        ptrs = ", ".join([f"const {t}* __restrict__"] * nptr)
+        for k in kernels:
+            lines.append(f"template __global__ void {k}<{t}>({a}, {a}, {ptrs});")
+        lines.append(f"template __global__ void rlfilter<{t}>({t}* __restrict__, const {t}* __restrict__, "
+                     f"const {t}* __restrict__);")
+    return "\n".join(lines) + "\n"
+
+
+# nvcc flags of torch's CUDAExtension build of the reference (setup.py), with the
+# architecture set to this GPU
+_REF_NVCC = ["-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-w",
+             "-D__CUDA_NO_HALF_OPERATORS__", "-D__CUDA_NO_HALF_CONVERSIONS__",
+             "-D__CUDA_NO_BFLOAT16_CONVERSIONS__", "-D__CUDA_NO_HALF2_OPERATORS__",
+             "--expt-relaxed-constexpr", "-DTORCH_EXTENSION_NAME=ctlib", "-DTORCH_API_INCLUDE_EXTENSION_H"]
+
+
+def build_ref_gpu(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> list[str] | None:
+    """Compile the reference kernels to compressed sm_103a cubins; None if no checkout."""
+    import gzip
+    import shutil
+    import sysconfig
+    srcdir = os.path.join(ref_root, "src")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.isdir(srcdir) or not os.path.exists(nvcc):
+        return None
+    try:
+        from torch.utils.cpp_extension import include_paths
+        incs = include_paths()
+    except Exception:
+        return None
+    incs = incs + [srcdir, sysconfig.get_paths()["include"]]
+    wdir = os.path.join(BUILD_DIR, "ref_gpu")
+    os.makedirs(wdir, exist_ok=True)
+    os.makedirs(REF_DIR, exist_ok=True)
+    jobs = []
+    for ns, fname in _KERNEL_FILES:
+        out = ref_cubin_path(ns)
+        if not (force or _stale(out, [os.path.join(srcdir, fname), os.path.abspath(__file__)])):
+            continue
+        wrapper = os.path.join(wdir, ns + ".cu")
+        with open(wrapper, "w") as f:
+            f.write(_ref_gpu_wrapper(ns, fname))
+        cubin = os.path.join(wdir, ns + ".cubin")
+        cmd = [nvcc, *_REF_NVCC, *[a for i in incs for a in ("-I", i)], "-D_GLIBCXX_USE_CXX11_ABI=1",
+               wrapper, "-o", cubin]
+        jobs.append((subprocess.Popen(cmd), cubin, out))
+    for proc, cubin, out in jobs:
+        if proc.wait() != 0:
+            raise RuntimeError(f"nvcc failed for {cubin}")
+        with open(cubin, "rb") as f, gzip.open(out + ".tmp", "wb") as g:
+            g.write(f.read())
+        os.replace(out + ".tmp", out)
+    return [ref_cubin_path(ns) for ns, _ in _KERNEL_FILES]
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_gpu(force="--force" in sys.argv))
