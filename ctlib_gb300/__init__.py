@@ -9,7 +9,7 @@ declared in ``include/ctgb.h``; there is no CPU path.
 """
 
 from .ops import (backprojection, backprojection_sv, backprojection_t, clear_plans, fbp, get_plan,  # noqa: F401
-                  projection, projection_t)
+                  laplacian, projection, projection_t)
 
 __all__ = ["projection", "projection_t", "backprojection", "backprojection_t", "fbp", "backprojection_sv",
-           "get_plan", "clear_plans"]
+           "laplacian", "get_plan", "clear_plans"]

@@ -19,11 +19,13 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD_DIR = os.path.join(PKG, "_build")
 SO_PATH = os.path.join(BUILD_DIR, "libctgb.so")
 INCLUDE = os.path.join(ROOT, "include")
-SOURCES = [os.path.join(CSRC, "ctgb_kernels.cu"), os.path.join(CSRC, "geometry.cpp")]
-HEADERS = [os.path.join(INCLUDE, "ctgb.h"), os.path.join(CSRC, "geometry.h")]
+SOURCES = [os.path.join(CSRC, "ctgb_kernels.cu"), os.path.join(CSRC, "ctgb_laplacian.cu"),
+           os.path.join(CSRC, "geometry.cpp")]
+HEADERS = [os.path.join(INCLUDE, "ctgb.h"), os.path.join(CSRC, "geometry.h"), os.path.join(CSRC, "ctgb_internal.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 OK, ERR_INVALID, ERR_CUDA, ERR_WORKSPACE = 0, 1, 2, 3
+FLOAT32, FLOAT64 = 0, 1
 OP_PROJECTION, OP_PROJECTION_T, OP_BACKPROJECTION, OP_BACKPROJECTION_T, OP_FBP = 0, 1, 2, 3, 4
 OP_BACKPROJECTION_SV = 5
 OP_DATA_GRADIENT = 6  # workspace queries of ctgb_data_gradient
@@ -91,6 +93,10 @@ def _declare(l):
         f.restype = c_int
     l.ctgb_data_gradient.argtypes = [vp, vp, vp, vp, vp, c_int, vp, c_size, vp]
     l.ctgb_data_gradient.restype = c_int
+    l.ctgb_laplacian_workspace_size.argtypes = [c_int, c_int, c_int, c_int]
+    l.ctgb_laplacian_workspace_size.restype = c_size
+    l.ctgb_laplacian.argtypes = [vp, c_int, c_int, c_int, c_int, vp, vp, vp, c_size, vp]
+    l.ctgb_laplacian.restype = c_int
     l.ctgb_projection_noalloc.argtypes = [vp, vp, vp, c_int, vp]
     l.ctgb_projection_noalloc.restype = c_int
     l.ctgb_projection_noalloc_max_bytes.argtypes = []
@@ -148,7 +154,8 @@ EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_pla
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",
             "ctgb_fbp", "ctgb_backprojection_sv", "ctgb_data_gradient", "ctgb_projection_noalloc", "ctgb_projection_noalloc_max_bytes", "ctgb_ragged_create",
             "ctgb_ragged_destroy", "ctgb_ragged_workspace_size", "ctgb_ragged_run", "ctgb_last_error",
-            "ctgb_version", "ctgb_geometry_query", "ctgb_wait_timeouts")
+            "ctgb_version", "ctgb_geometry_query", "ctgb_wait_timeouts", "ctgb_laplacian_workspace_size",
+            "ctgb_laplacian")
 
 
 def wait_timeouts(device: int = 0, reset: bool = False) -> int:

@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "ctgb.h"
+#include "ctgb_internal.h"
 #include "geometry.h"
 
 namespace ctgb {
@@ -47,7 +48,7 @@ namespace ctgb {
 // ----------------------------------------------------------------------------
 static thread_local std::string g_err;
 
-static int fail(int code, const std::string& msg) {
+int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }

@@ -1,0 +1,450 @@
+// kNN graph adjacency of CTLIB's `laplacian` (src/laplacian_cuda_kernel.cu:46-128,
+// src/ctlib.cpp:101-104) for GB300 (sm_103a), behind ctgb_laplacian in ctgb.h.
+//
+// For n points x_i of dimension dim the reference builds the full n x n matrix
+// dist[i][j] = |x_i|^2 + |x_j|^2 - 2 <x_i, x_j> (a norm kernel, a norm-sum
+// kernel and a GEMM), takes the k smallest entries of every row with
+// torch::topk, divides them by the median of all n*k selected distances,
+// applies exp(-.), normalises each row to sum 1 and returns a sparse COO
+// matrix with float32 values.
+//
+// Here the n x n matrix never exists. One kernel computes 64 x 128 tiles of
+// distances from shared-memory chunks of the points (register-blocked FP32 or
+// FP64 FMAs) and folds each tile straight into per-row sorted lists of the k
+// best (distance, column) pairs in shared memory; column ranges are split over
+// CTAs to fill the GPU and the partial lists merged. The lists are ordered by
+// distance, then by column index, so the selected set and its order do not
+// depend on the tile schedule or the split (ties go to the smaller index). The
+// median is a radix select over the n*k selected distances (the lower median,
+// as torch::median) and a last kernel writes the COO indices and weights.
+//
+// Traffic: the points are read once per 128-column tile from L2; HBM sees the
+// points, the n*k lists and the output, instead of 2 n^2 distances.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "ctgb.h"
+#include "ctgb_internal.h"
+
+namespace ctgb {
+namespace lap {
+
+constexpr int TM = 64;    // rows (points i) per CTA
+constexpr int TN = 128;   // columns (points j) per tile
+constexpr int DC = 32;    // dimension chunk staged in shared memory
+constexpr int NT = 256;   // threads per CTA: 16 x 16, 4 rows x 8 columns each
+constexpr int SA = TM + 4, SBW = TN + 4, SD = TN + 4;  // padded row strides (16-byte multiples)
+constexpr int kMaxSplit = 8;
+constexpr int kMaxK = 256;
+
+template <class T>
+__device__ __forceinline__ bool lexless(T av, int ai, T bv, int bi) {
+  return av < bv || (av == bv && ai < bi);
+}
+
+template <class T>
+__device__ __forceinline__ void ld4s(const T* p, T* v) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  } else {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+}
+
+// |x_i|^2 in the reference's order: sum += v * v over the dimension, one FMA
+// per term (src/laplacian_cuda_kernel.cu:10-22)
+template <class T>
+__global__ void k_sqnorm(const T* __restrict__ x, int n, int dim, T* __restrict__ norm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T* r = x + (size_t)i * dim;
+  T s = T(0);
+  for (int d = 0; d < dim; ++d) s = fma(r[d], r[d], s);
+  norm[i] = s;
+}
+
+// Insert (cv, cj) into the sorted list (Lv, Li) of K entries, dropping the
+// last one; the whole warp takes part. The caller guarantees that (cv, cj)
+// precedes the last entry.
+template <class T>
+__device__ __forceinline__ void list_insert(T* Lv, int* Li, int K, T cv, int cj, int lane) {
+  int p = 0;
+  for (int e0 = 0; e0 < K; e0 += 32) {
+    const int e = e0 + lane;
+    const bool less = e < K && lexless(Lv[e], Li[e], cv, cj);
+    p += __popc(__ballot_sync(0xffffffffu, less));
+  }
+  // shift [p, K-2] up by one, highest chunk first so no entry is overwritten
+  // before it is read
+  const int nmove = K - 1 - p;
+  for (int m = nmove > 0 ? (nmove - 1) / 32 : -1; m >= 0; --m) {
+    const int e = p + 1 + lane + 32 * m;
+    const bool act = e <= K - 1;
+    T v = T(0);
+    int ix = 0;
+    if (act) { v = Lv[e - 1]; ix = Li[e - 1]; }
+    __syncwarp();
+    if (act) { Lv[e] = v; Li[e] = ix; }
+    __syncwarp();
+  }
+  if (lane == 0) { Lv[p] = cv; Li[p] = cj; }
+  __syncwarp();
+}
+
+template <class T>
+size_t knn_smem_bytes(int K) {
+  return ((size_t)DC * SA + (size_t)DC * SBW + (size_t)TM * SD + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
+}
+
+// Rows [i0, i0 + TM) against columns [c_begin, c_end): the K smallest
+// (distance, column) pairs of each row, sorted, into out_v / out_i at
+// [(row * nsplit + split) * K]. dist = fma(-2, <x_i, x_j>, |x_j|^2 + |x_i|^2),
+// the reference's norm sum with the GEMM's -2 x^T x added
+// (src/laplacian_cuda_kernel.cu:25-43, 88-106).
+template <class T>
+__global__ void __launch_bounds__(NT) k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim,
+                                            int K, int cols_per_split, int nsplit, T* __restrict__ out_v,
+                                            int* __restrict__ out_i) {
+  extern __shared__ __align__(16) unsigned char lap_smem[];
+  T* sA = reinterpret_cast<T*>(lap_smem);  // [DC][SA]: x_i chunk, transposed
+  T* sB = sA + DC * SA;                     // [DC][SBW]: x_j chunk, transposed
+  T* sD = sB + DC * SBW;                    // [TM][SD]: one tile of distances
+  T* lv = sD + TM * SD;                     // [TM][K]: list values
+  int* li = reinterpret_cast<int*>(lv + TM * K);  // [TM][K]: list columns
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int i0 = blockIdx.x * TM;
+  const int split = blockIdx.y;
+  const int c_begin = split * cols_per_split;
+  const int c_end = min(n, c_begin + cols_per_split);
+  const T inf = T(INFINITY);
+  for (int e = tid; e < TM * K; e += NT) { lv[e] = inf; li[e] = INT_MAX; }
+  T ni[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int r = i0 + ty * 4 + a;
+    ni[a] = r < n ? norm[r] : T(0);
+  }
+  for (int j0 = c_begin; j0 < c_end; j0 += TN) {
+    T acc[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = T(0);
+    for (int k0 = 0; k0 < dim; k0 += DC) {
+      const int kc = min(DC, dim - k0);
+      __syncthreads();  // the previous chunk and the previous tile's selection are done
+      for (int e = tid; e < TM * DC; e += NT) {
+        const int r = e / DC, kk = e % DC;
+        const int gi = i0 + r;
+        sA[kk * SA + r] = (gi < n && kk < kc) ? x[(size_t)gi * dim + k0 + kk] : T(0);
+      }
+      for (int e = tid; e < TN * DC; e += NT) {
+        const int c = e / DC, kk = e % DC;
+        const int gj = j0 + c;
+        sB[kk * SBW + c] = (gj < c_end && kk < kc) ? x[(size_t)gj * dim + k0 + kk] : T(0);
+      }
+      __syncthreads();
+      for (int kk = 0; kk < kc; ++kk) {
+        T av[4], bv[8];
+        ld4s<T>(sA + kk * SA + ty * 4, av);
+        ld4s<T>(sB + kk * SBW + tx * 4, bv);
+        ld4s<T>(sB + kk * SBW + 64 + tx * 4, bv + 4);
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 8; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+      }
+    }
+    // distances of the tile; columns past the range are NaN, which no
+    // comparison selects
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int c = b < 4 ? tx * 4 + b : 64 + tx * 4 + (b - 4);
+      const int gj = j0 + c;
+      const T nj = gj < c_end ? norm[gj] : T(0);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+        sD[(ty * 4 + a) * SD + c] = gj < c_end ? fma(T(-2), acc[a][b], nj + ni[a]) : T(NAN);
+    }
+    __syncthreads();
+    // selection: warp w owns rows 8w .. 8w+7 of the block for the whole kernel
+    for (int rr = 0; rr < TM / 8; ++rr) {
+      const int r = warp * (TM / 8) + rr;
+      if (i0 + r >= n) break;
+      T* Lv = lv + r * K;
+      int* Li = li + r * K;
+      T tv = Lv[K - 1];
+      int ti = Li[K - 1];
+#pragma unroll
+      for (int q = 0; q < TN / 32; ++q) {
+        const int c = q * 32 + lane;
+        const T dv = sD[r * SD + c];
+        const int j = j0 + c;
+        bool pass = lexless(dv, j, tv, ti);
+        unsigned m = __ballot_sync(0xffffffffu, pass);
+        while (m) {
+          const int src = __ffs(m) - 1;
+          const T cv = __shfl_sync(0xffffffffu, dv, src);
+          const int cj = __shfl_sync(0xffffffffu, j, src);
+          list_insert<T>(Lv, Li, K, cv, cj, lane);
+          tv = Lv[K - 1];
+          ti = Li[K - 1];
+          if (lane == src) pass = false;
+          pass = pass && lexless(dv, j, tv, ti);
+          m = __ballot_sync(0xffffffffu, pass);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int rr = 0; rr < TM / 8; ++rr) {
+    const int r = warp * (TM / 8) + rr;
+    const int gi = i0 + r;
+    if (gi >= n) break;
+    const size_t o = ((size_t)gi * nsplit + split) * K;
+    for (int e = lane; e < K; e += 32) {
+      out_v[o + e] = lv[r * K + e];
+      out_i[o + e] = li[r * K + e];
+    }
+  }
+}
+
+// merge the nsplit sorted partial lists of each row into its K best
+template <class T>
+__global__ void k_knn_merge(const T* __restrict__ pv, const int* __restrict__ pi, int n, int nsplit, int K,
+                            T* __restrict__ fv, int* __restrict__ fi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pos[kMaxSplit];
+#pragma unroll
+  for (int s = 0; s < kMaxSplit; ++s) pos[s] = 0;
+  for (int e = 0; e < K; ++e) {
+    int best = 0;
+    T bv = T(0);
+    int bi = INT_MAX;
+    bool have = false;
+#pragma unroll
+    for (int s = 0; s < kMaxSplit; ++s) {
+      if (s < nsplit && pos[s] < K) {
+        const size_t o = ((size_t)i * nsplit + s) * K + pos[s];
+        const T v = pv[o];
+        const int ix = pi[o];
+        if (!have || lexless(v, ix, bv, bi)) { best = s; bv = v; bi = ix; have = true; }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < kMaxSplit; ++s) pos[s] += s == best;
+    fv[(size_t)i * K + e] = bv;
+    fi[(size_t)i * K + e] = bi;
+  }
+}
+
+// ordered unsigned keys of floating-point values (sign-magnitude flipped)
+template <class T>
+struct Key;
+template <>
+struct Key<float> {
+  using U = unsigned int;
+  static constexpr int kPasses = 4;
+  __device__ static U enc(float v) {
+    const U u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  }
+  __device__ static float dec(U k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
+};
+template <>
+struct Key<double> {
+  using U = unsigned long long;
+  static constexpr int kPasses = 8;
+  __device__ static U enc(double v) {
+    const U u = (U)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | (1ull << 63));
+  }
+  __device__ static double dec(U k) { return __longlong_as_double((long long)((k >> 63) ? (k & ~(1ull << 63)) : ~k)); }
+};
+
+struct SelectState {
+  unsigned long long prefix, mask, rank;
+  unsigned int hist[256];
+  unsigned int ticket;
+};
+
+__global__ void k_select_init(SelectState* st, unsigned long long rank) {
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) st->hist[b] = 0;
+  if (threadIdx.x == 0) { st->prefix = 0; st->mask = 0; st->rank = rank; st->ticket = 0; }
+}
+
+// One 8-bit digit (most significant first) of the radix select of the value of
+// rank st->rank among v[0, m). Every CTA histograms the digit of the values
+// that match the digits found so far; the last CTA to finish (ticket) picks the
+// digit, resets the histogram, and after the last digit writes the value.
+template <class T>
+__global__ void __launch_bounds__(256) k_select_pass(const T* __restrict__ v, size_t m, int shift, SelectState* st,
+                                                     T* __restrict__ out) {
+  using U = typename Key<T>::U;
+  __shared__ unsigned int h[256];
+  __shared__ bool last;
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  const U prefix = (U)st->prefix, mask = (U)st->mask;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < m; e += (size_t)gridDim.x * blockDim.x) {
+    const U key = Key<T>::enc(v[e]);
+    if ((key & mask) == prefix) atomicAdd(&h[(unsigned)(key >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 256; b += blockDim.x)
+    if (h[b]) atomicAdd(&st->hist[b], h[b]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  volatile unsigned int* hist = st->hist;
+  unsigned long long rank = st->rank;
+  int b = 0;
+  for (; b < 255; ++b) {
+    const unsigned int c = hist[b];
+    if (rank < c) break;
+    rank -= c;
+  }
+  const U np = prefix | ((U)b << shift);
+  st->prefix = np;
+  st->mask = mask | ((U)255 << shift);
+  st->rank = rank;
+  for (int i = 0; i < 256; ++i) hist[i] = 0;
+  st->ticket = 0;
+  if (shift == 0) *out = Key<T>::dec(np);
+}
+
+__device__ __forceinline__ float exp_t(float v) { return expf(v); }
+__device__ __forceinline__ double exp_t(double v) { return exp(v); }
+
+// weights of row i: exp(-(d / median)), normalised to sum 1, as float32 with
+// COO indices (i, j) (src/laplacian_cuda_kernel.cu:112-126)
+template <class T>
+__global__ void k_lap_weights(const T* __restrict__ fv, const int* __restrict__ fi, int n, int K,
+                              const T* __restrict__ med, long long* __restrict__ ind, float* __restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T md = *med;
+  const T* d = fv + (size_t)i * K;
+  T s = T(0);
+  for (int e = 0; e < K; ++e) s += exp_t(-(d[e] / md));
+  const size_t nk = (size_t)n * K;
+  for (int e = 0; e < K; ++e) {
+    const size_t o = (size_t)i * K + e;
+    val[o] = (float)(exp_t(-(d[e] / md)) / s);
+    ind[o] = i;
+    ind[nk + o] = fi[o];
+  }
+}
+
+struct Layout {
+  int nsplit, cols_per_split;
+  size_t off_norm, off_pv, off_pi, off_fv, off_fi, off_state, off_med, total;
+};
+
+inline size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+inline Layout layout(int n, int k, size_t es) {
+  Layout L{};
+  const int rowblocks = (n + TM - 1) / TM;
+  int ns = std::max(1, std::min(kMaxSplit, (2 * 152 + rowblocks - 1) / rowblocks));
+  int cps = (n + ns - 1) / ns;
+  cps = (cps + TN - 1) / TN * TN;
+  ns = (n + cps - 1) / cps;
+  L.nsplit = ns;
+  L.cols_per_split = cps;
+  size_t off = 0;
+  L.off_norm = off; off = al256(off + (size_t)n * es);
+  const size_t nk = (size_t)n * k;
+  if (ns > 1) {
+    L.off_pv = off; off = al256(off + nk * ns * es);
+    L.off_pi = off; off = al256(off + nk * ns * 4);
+  }
+  L.off_fv = off; off = al256(off + nk * es);
+  L.off_fi = off; off = al256(off + nk * 4);
+  L.off_state = off; off = al256(off + sizeof(SelectState));
+  L.off_med = off; off = al256(off + es);
+  L.total = off;
+  return L;
+}
+
+template <class T>
+int run(const T* x, int n, int dim, int k, long long* ind, float* val, unsigned char* ws, cudaStream_t st) {
+  const Layout L = layout(n, k, sizeof(T));
+  T* norm = reinterpret_cast<T*>(ws + L.off_norm);
+  T* fv = reinterpret_cast<T*>(ws + L.off_fv);
+  int* fi = reinterpret_cast<int*>(ws + L.off_fi);
+  T* pv = L.nsplit > 1 ? reinterpret_cast<T*>(ws + L.off_pv) : fv;
+  int* pi = L.nsplit > 1 ? reinterpret_cast<int*>(ws + L.off_pi) : fi;
+  SelectState* sel = reinterpret_cast<SelectState*>(ws + L.off_state);
+  T* med = reinterpret_cast<T*>(ws + L.off_med);
+  const size_t smem = knn_smem_bytes<T>(k);
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian: ") + cudaGetErrorString(e));
+  if (smem > (size_t)optin)
+    return fail(CTGB_ERR_INVALID, "laplacian: k too large for this dtype (" + std::to_string(smem) +
+                                      " bytes of shared memory per CTA needed)");
+  e = cudaFuncSetAttribute(k_knn<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian smem: ") + cudaGetErrorString(e));
+  k_sqnorm<T><<<(n + 255) / 256, 256, 0, st>>>(x, n, dim, norm);
+  dim3 grid((n + TM - 1) / TM, L.nsplit);
+  k_knn<T><<<grid, NT, smem, st>>>(x, norm, n, dim, k, L.cols_per_split, L.nsplit, pv, pi);
+  if (L.nsplit > 1) k_knn_merge<T><<<(n + 127) / 128, 128, 0, st>>>(pv, pi, n, L.nsplit, k, fv, fi);
+  const size_t m = (size_t)n * k;
+  k_select_init<<<1, 256, 0, st>>>(sel, (m - 1) / 2);
+  const int sb = (int)std::max<size_t>(1, std::min<size_t>((m + 2047) / 2048, 152 * 4));
+  for (int p = Key<T>::kPasses - 1; p >= 0; --p) k_select_pass<T><<<sb, 256, 0, st>>>(fv, m, 8 * p, sel, med);
+  k_lap_weights<T><<<(n + 127) / 128, 128, 0, st>>>(fv, fi, n, k, med, ind, val);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian launch: ") + cudaGetErrorString(e));
+  return CTGB_OK;
+}
+
+}  // namespace lap
+}  // namespace ctgb
+
+extern "C" {
+
+size_t ctgb_laplacian_workspace_size(int n, int dim, int k, int dtype) {
+  if (n < 1 || dim < 1 || k < 1 || k > n || (dtype != CTGB_FLOAT32 && dtype != CTGB_FLOAT64)) return 0;
+  return ctgb::lap::layout(n, k, dtype == CTGB_FLOAT32 ? 4 : 8).total;
+}
+
+int ctgb_laplacian(const void* points, int n, int dim, int k, int dtype, long long* indices, float* values,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace ctgb;
+  if (dtype != CTGB_FLOAT32 && dtype != CTGB_FLOAT64) return fail(CTGB_ERR_INVALID, "laplacian: bad dtype");
+  if (n < 1 || dim < 1) return fail(CTGB_ERR_INVALID, "laplacian: need at least one point of dimension >= 1");
+  if (k < 1 || k > n) return fail(CTGB_ERR_INVALID, "laplacian: k must be in [1, n]");
+  if (k > lap::kMaxK) return fail(CTGB_ERR_INVALID, "laplacian: k > 256 is not supported");
+  if ((size_t)n * (size_t)k > (size_t)INT_MAX) return fail(CTGB_ERR_INVALID, "laplacian: n * k too large");
+  if (!points || !indices || !values || !workspace) return fail(CTGB_ERR_INVALID, "laplacian: null pointer");
+  if ((reinterpret_cast<uintptr_t>(workspace) & 255) != 0)
+    return fail(CTGB_ERR_INVALID, "workspace must be 256-byte aligned");
+  const size_t es = dtype == CTGB_FLOAT32 ? 4 : 8;
+  if ((reinterpret_cast<uintptr_t>(points) & (es - 1)) != 0)
+    return fail(CTGB_ERR_INVALID, "laplacian: points not aligned to their element size");
+  if (workspace_bytes < lap::layout(n, k, es).total) return fail(CTGB_ERR_WORKSPACE, "laplacian: workspace too small");
+  auto* ws = static_cast<unsigned char*>(workspace);
+  auto st = static_cast<cudaStream_t>(stream);
+  if (dtype == CTGB_FLOAT32)
+    return lap::run<float>(static_cast<const float*>(points), n, dim, k, indices, values, ws, st);
+  return lap::run<double>(static_cast<const double*>(points), n, dim, k, indices, values, ws, st);
+}
+
+}  // extern "C"

@@ -267,3 +267,43 @@ def data_gradient(image: torch.Tensor, projection: torch.Tensor, options, return
                                             ws.data_ptr(), ctypes.c_size_t(nbytes), stream.cuda_stream)
         N.check(rc, "data_gradient")
     return (grad, res) if return_residual else grad
+
+
+def laplacian(input: torch.Tensor, k: int) -> torch.Tensor:
+    """kNN graph adjacency of the n rows of an n x dim tensor (src/ctlib.cpp:101-104,
+    src/laplacian_cuda_kernel.cu:46-128): for every point its k nearest points,
+    itself included, weighted exp(-d / m) with d the squared distance and m the
+    lower median of all n*k selected distances, normalised to sum 1 per row.
+    Returns an n x n sparse COO tensor with float32 values, neighbours of each
+    row in increasing distance (ctgb_laplacian). Ties in distance go to the
+    smaller index; k <= 256."""
+    import ctypes
+    if not isinstance(input, torch.Tensor):
+        raise TypeError("input must be a torch.Tensor")
+    if not input.is_cuda:
+        raise RuntimeError("input must be a CUDA tensor")
+    if not input.is_contiguous():
+        raise RuntimeError("input must be contiguous")
+    if input.dtype not in _FLOATS:
+        raise RuntimeError(f"input must be float32 or float64, got {input.dtype}")
+    if input.dim() != 2:
+        raise ValueError(f"input must be 2-D (points x dimension), got shape {tuple(input.shape)}")
+    n, dim = (int(s) for s in input.shape)
+    k = int(k)
+    if n < 1 or dim < 1:
+        raise ValueError("input must hold at least one point of dimension >= 1")
+    if not 1 <= k <= n:
+        raise ValueError(f"k must be in [1, {n}], got {k}")
+    if k > 256:
+        raise ValueError("k > 256 is not supported")
+    dt = N.FLOAT32 if input.dtype == torch.float32 else N.FLOAT64
+    nbytes = int(N.lib().ctgb_laplacian_workspace_size(n, dim, k, dt))
+    ind = torch.empty((2, n * k), dtype=torch.int64, device=input.device)
+    val = torch.empty((n * k,), dtype=torch.float32, device=input.device)
+    with torch.cuda.device(input.device):
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=input.device)
+        stream = torch.cuda.current_stream(input.device)
+        rc = N.lib().ctgb_laplacian(input.data_ptr(), n, dim, k, dt, ind.data_ptr(), val.data_ptr(),
+                                    ws.data_ptr(), ctypes.c_size_t(nbytes), stream.cuda_stream)
+    N.check(rc, "laplacian")
+    return torch.sparse_coo_tensor(ind, val, (n, n), dtype=torch.float32, device=input.device)

@@ -201,6 +201,20 @@ const char* ctgb_last_error(void);
  * in the reference. */
 int ctgb_wait_timeouts(int device, unsigned long long* count, int reset);
 
+/* kNN graph adjacency (replaces `laplacian`, src/ctlib.cpp:101-104 and
+ * src/laplacian_cuda_kernel.cu:46-128). `points` is an n x dim row-major device
+ * array of `dtype`. For every point i the k smallest squared distances
+ * |x_i|^2 + |x_j|^2 - 2 <x_i, x_j> (i itself included, ties to the smaller j)
+ * are weighted exp(-d / m), m the lower median of all n*k selected distances,
+ * and normalised to sum 1 per row. Output, the reference's COO layout:
+ * indices[0][i*k + e] = i, indices[1][i*k + e] = j_e (int64, 2 x n*k) and
+ * values[i*k + e] (float32 for either dtype, as the reference's sparse tensor),
+ * neighbours in increasing distance. 1 <= k <= min(n, 256); runs on the
+ * current device. The n x n distance matrix is never formed. */
+size_t ctgb_laplacian_workspace_size(int n, int dim, int k, int dtype);
+int ctgb_laplacian(const void* points, int n, int dim, int k, int dtype, long long* indices, float* values,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
 /* ABI version, bumped on incompatible changes. */
 int ctgb_version(void);
 

@@ -15,7 +15,8 @@
   harmless because all warps read before any writes, but which a one-thread-at-
   a-time execution would otherwise turn into a real read-after-write.
 
-* ``build_ref_gpu()`` compiles the same three reference files for the GPU, as
+* ``build_ref_gpu()`` compiles the same three reference files, and the
+  graph-Laplacian kernels of ``src/laplacian_cuda_kernel.cu``, for the GPU, as
   the reference's ``CUDAExtension`` does but for sm_103a, into
   ``oracle/_ref/ref_<file>.cubin.gz``, which ``ref_cuda.py`` loads through the
   CUDA driver API. A generated wrapper (``oracle/_build/ref_gpu/*.cu``)
@@ -132,13 +133,16 @@ REF_GPU_KERNELS = {
 }
 
 
+# the graph-Laplacian file (src/laplacian_cuda_kernel.cu:10-43): two kernels on a
+# 2-D accessor; its GEMM is a cuBLAS call replayed by ref_cuda.py
+REF_GPU_LAPLACIAN = ("ref_laplacian", "laplacian_cuda_kernel.cu")
+
+
 def ref_cubin_path(ns: str) -> str:
     return os.path.join(REF_DIR, f"{ns}.cubin.gz")
 
 
 def _ref_gpu_wrapper(ns: str, fname: str) -> str:
-    kernels, nptr = REF_GPU_KERNELS[ns]
-    acc = "torch::PackedTensorAccessor<T, 4, torch::RestrictPtrTraits, size_t>"
     lines = [
         "// Written by oracle/build.py: the reference's kernels of " + fname + ",",
         "// included by name from the checkout, instantiated for float and double.",
@@ -148,6 +152,14 @@ def _ref_gpu_wrapper(ns: str, fname: str) -> str:
         "#define AT_DISPATCH_FLOATING_TYPES(TYPE, NAME, ...)",
         f'#include "{fname}"',
     ]
+    if ns == REF_GPU_LAPLACIAN[0]:
+        for t in ("float", "double"):
+            a2 = f"torch::PackedTensorAccessor<{t}, 2, torch::RestrictPtrTraits, size_t>"
+            lines.append(f"template __global__ void compute_squared_norm<{t}>({a2}, int, int, {t}* __restrict__);")
+            lines.append(f"template __global__ void add_norm<{t}>({a2}, int, {t}* __restrict__);")
+        return "\n".join(lines) + "\n"
+    kernels, nptr = REF_GPU_KERNELS[ns]
+    acc = "torch::PackedTensorAccessor<T, 4, torch::RestrictPtrTraits, size_t>"
     for t in ("float", "double"):
         a = acc.replace("<T,", f"<{t},")
         ptrs = ", ".join([f"const {t}* __restrict__"] * nptr)
@@ -185,7 +197,7 @@ def build_ref_gpu(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> list
     os.makedirs(wdir, exist_ok=True)
     os.makedirs(REF_DIR, exist_ok=True)
     jobs = []
-    for ns, fname in _KERNEL_FILES:
+    for ns, fname in _KERNEL_FILES + (REF_GPU_LAPLACIAN,):
         out = ref_cubin_path(ns)
         if not (force or _stale(out, [os.path.join(srcdir, fname), os.path.abspath(__file__)])):
             continue
@@ -202,7 +214,7 @@ def build_ref_gpu(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> list
         with open(cubin, "rb") as f, gzip.open(out + ".tmp", "wb") as g:
             g.write(f.read())
         os.replace(out + ".tmp", out)
-    return [ref_cubin_path(ns) for ns, _ in _KERNEL_FILES]
+    return [ref_cubin_path(ns) for ns, _ in _KERNEL_FILES + (REF_GPU_LAPLACIAN,)]
 
 
 if __name__ == "__main__":

@@ -52,6 +52,10 @@ def available() -> bool:
     return all(os.path.exists(_build.ref_cubin_path(ns)) for ns in SCAN_NS.values())
 
 
+def laplacian_available() -> bool:
+    return os.path.exists(_build.ref_cubin_path(_build.REF_GPU_LAPLACIAN[0]))
+
+
 class _Driver:
     def __init__(self):
         self.lib = ctypes.CDLL("libcuda.so.1")
@@ -117,22 +121,28 @@ class RefCuda:
         self.checked = set()
         self._modules = []
         for scan, ns in SCAN_NS.items():
-            with gzip.open(_build.ref_cubin_path(ns), "rb") as f:
-                image = f.read()
-            buf = ctypes.create_string_buffer(image, len(image))
-            mod = ctypes.c_void_p()
-            self.drv.check(self.drv.lib.cuModuleLoadData(ctypes.byref(mod), buf), f"cuModuleLoadData({ns})")
-            self._modules.append((mod, buf))
-            cnt = ctypes.c_uint()
-            self.drv.check(self.drv.lib.cuModuleGetFunctionCount(ctypes.byref(cnt), mod), "cuModuleGetFunctionCount")
-            arr = (ctypes.c_void_p * cnt.value)()
-            self.drv.check(self.drv.lib.cuModuleEnumerateFunctions(arr, cnt.value, mod), "cuModuleEnumerateFunctions")
-            for fn in arr:
-                nm = ctypes.c_char_p()
-                self.drv.check(self.drv.lib.cuFuncGetName(ctypes.byref(nm), fn), "cuFuncGetName")
-                head = _demangle_head(nm.value.decode())
-                if head is not None:
-                    self.funcs[(scan,) + head] = ctypes.c_void_p(fn)
+            self._load_module(scan, ns)
+        if laplacian_available():
+            self._load_module("laplacian", _build.REF_GPU_LAPLACIAN[0])
+        self._cublas = None
+
+    def _load_module(self, key, ns):
+        with gzip.open(_build.ref_cubin_path(ns), "rb") as f:
+            image = f.read()
+        buf = ctypes.create_string_buffer(image, len(image))
+        mod = ctypes.c_void_p()
+        self.drv.check(self.drv.lib.cuModuleLoadData(ctypes.byref(mod), buf), f"cuModuleLoadData({ns})")
+        self._modules.append((mod, buf))
+        cnt = ctypes.c_uint()
+        self.drv.check(self.drv.lib.cuModuleGetFunctionCount(ctypes.byref(cnt), mod), "cuModuleGetFunctionCount")
+        arr = (ctypes.c_void_p * cnt.value)()
+        self.drv.check(self.drv.lib.cuModuleEnumerateFunctions(arr, cnt.value, mod), "cuModuleEnumerateFunctions")
+        for fn in arr:
+            nm = ctypes.c_char_p()
+            self.drv.check(self.drv.lib.cuFuncGetName(ctypes.byref(nm), fn), "cuFuncGetName")
+            head = _demangle_head(nm.value.decode())
+            if head is not None:
+                self.funcs[(key,) + head] = ctypes.c_void_p(fn)
 
     # -- parameter checks ------------------------------------------------------
     def _check_params(self, fn, key, sizes):
@@ -143,7 +153,8 @@ class RefCuda:
             off, size = ctypes.c_size_t(), ctypes.c_size_t()
             self.drv.check(self.drv.lib.cuFuncGetParamInfo(fn, i, ctypes.byref(off), ctypes.byref(size)),
                            f"cuFuncGetParamInfo({key}, {i})")
-            off_expect = (off_expect + 7) // 8 * 8
+            al = min(s, 8)
+            off_expect = (off_expect + al - 1) // al * al
             if size.value != s or off.value != off_expect:
                 raise RuntimeError(f"{key}: parameter {i} is {size.value} bytes at {off.value}, "
                                    f"expected {s} at {off_expect}")
@@ -167,8 +178,9 @@ class RefCuda:
         return (ctypes.c_uint64 * 9)(t.data_ptr(), *[int(s) for s in t.shape], *[int(s) for s in t.stride()])
 
     def _launch(self, fn, grid, block, args, stream):
+        bx, by = (block, 1) if isinstance(block, int) else block
         params = (ctypes.c_void_p * len(args))(*[ctypes.cast(ctypes.pointer(a), ctypes.c_void_p) for a in args])
-        self.drv.check(self.drv.lib.cuLaunchKernel(fn, grid[0], grid[1], grid[2], block, 1, 1, 0,
+        self.drv.check(self.drv.lib.cuLaunchKernel(fn, grid[0], grid[1], grid[2], bx, by, 1, 0,
                                                    ctypes.c_void_p(stream), params, None), "cuLaunchKernel")
 
     # -- operators -------------------------------------------------------------
@@ -270,6 +282,92 @@ class RefCuda:
         filtered = torch.nn.functional.conv2d(weighted, filt, None, 1, (0, D - 1)).contiguous()
         image = self.run(2, filtered, options)
         return image * o[7] / 2
+
+    def laplacian(self, x, k: int):
+        """The reference's laplacian (src/laplacian_cuda_kernel.cu:46-128) step by
+        step: its compute_squared_norm and add_norm kernels (grids of 256 threads
+        and of 16 x 16 threads), cuBLAS ``gemm(T, N, n, n, dim, -2, x, dim, x, dim,
+        1, dist, n)`` on a fresh handle, then torch's topk, median, exp, row sums
+        and a float32 sparse COO tensor."""
+        torch = self.torch
+        if not laplacian_available() or ("laplacian", "add_norm", "f") not in self.funcs:
+            raise RuntimeError("reference laplacian cubin not built")
+        if x.dim() != 2 or not x.is_contiguous() or x.dtype not in (torch.float32, torch.float64):
+            raise ValueError("contiguous 2-D float32 or float64 points expected")
+        n, dim = (int(v) for v in x.shape)
+        if not 1 <= k <= n:
+            raise ValueError("k must be in [1, n]")
+        if self._cublas is None:
+            self._cublas = _Cublas(torch, self.device)
+        cb = self._cublas.lib
+        f32 = x.dtype == torch.float32
+        tcode = "f" if f32 else "d"
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        norm2 = torch.empty(n, dtype=x.dtype, device=self.device)
+        dist = torch.empty((n, n), dtype=x.dtype, device=self.device)
+        fn = self._kernel("laplacian", "compute_squared_norm", tcode, [40, 4, 4, 8])
+        self._launch(fn, (math.ceil(n / 256), 1, 1), 256,
+                     [_acc2(x), ctypes.c_int(n), ctypes.c_int(dim), ctypes.c_uint64(norm2.data_ptr())], stream)
+        fn = self._kernel("laplacian", "add_norm", tcode, [40, 4, 8])
+        nb = math.ceil(n / 16)
+        self._launch(fn, (nb, nb, 1), (16, 16), [_acc2(dist), ctypes.c_int(n), ctypes.c_uint64(norm2.data_ptr())],
+                     stream)
+        h = ctypes.c_void_p()
+        if cb.cublasCreate_v2(ctypes.byref(h)) != 0:
+            raise RuntimeError("cublasCreate failed")
+        try:
+            t = ctypes.c_float if f32 else ctypes.c_double
+            gemm = cb.cublasSgemm_v2 if f32 else cb.cublasDgemm_v2
+            alpha, beta = t(-2.0), t(1.0)
+            rc = gemm(h, 1, 0, n, n, dim, ctypes.byref(alpha), ctypes.c_void_p(x.data_ptr()), dim,
+                      ctypes.c_void_p(x.data_ptr()), dim, ctypes.byref(beta), ctypes.c_void_p(dist.data_ptr()), n)
+            if rc != 0:
+                raise RuntimeError(f"cuBLAS gemm failed: {rc}")
+        finally:
+            cb.cublasDestroy_v2(h)
+        coef, indj = torch.topk(dist, k, 1, False)
+        median = torch.median(coef)
+        coef = coef / median
+        coef = torch.exp(-coef)
+        coef = coef / coef.sum(1, True)
+        coef = coef.view(-1)
+        indi = torch.arange(n, dtype=torch.int64, device=self.device).unsqueeze_(1).repeat(1, k)
+        ind1 = torch.stack([indi, indj]).view(2, -1)
+        return torch.sparse_coo_tensor(ind1, coef, (n, n), dtype=torch.float32, device=self.device)
+
+class _Cublas:
+    """The cuBLAS library that PyTorch loaded (found through the process's
+    mapped files after one matmul), for the reference's GEMM calls."""
+
+    def __init__(self, torch, device):
+        a = torch.ones(2, 2, device=device)
+        (a @ a).sum().item()
+        path = None
+        with open("/proc/self/maps") as f:
+            for line in f:
+                part = line.split()[-1]
+                if "libcublas.so" in os.path.basename(part):
+                    path = part
+                    break
+        if path is None:
+            raise RuntimeError("libcublas not loaded by torch")
+        L = self.lib = ctypes.CDLL(path)
+        vp, ci = ctypes.c_void_p, ctypes.c_int
+        L.cublasCreate_v2.argtypes = [ctypes.POINTER(vp)]
+        L.cublasDestroy_v2.argtypes = [vp]
+        for name, t in (("cublasSgemm_v2", ctypes.c_float), ("cublasDgemm_v2", ctypes.c_double)):
+            fn = getattr(L, name)
+            fn.argtypes = [vp, ci, ci, ci, ci, ci, ctypes.POINTER(t), vp, ci, vp, ci, ctypes.POINTER(t), vp, ci]
+            fn.restype = ci
+        L.cublasCreate_v2.restype = ci
+        L.cublasDestroy_v2.restype = ci
+
+
+def _acc2(t):
+    assert t.dim() == 2 and t.is_contiguous()
+    return (ctypes.c_uint64 * 5)(t.data_ptr(), *[int(s) for s in t.shape], *[int(s) for s in t.stride()])
+
+
 
 
 def get() -> RefCuda:
