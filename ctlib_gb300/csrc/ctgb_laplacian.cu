@@ -10,9 +10,10 @@
 //
 // Here the n x n matrix never exists. One kernel computes 64 x 128 tiles of
 // distances from shared-memory chunks of the points (register-blocked FP32 or
-// FP64 FMAs) and folds each tile straight into per-row sorted lists of the k
-// best (distance, column) pairs in shared memory; column ranges are split over
-// CTAs to fill the GPU and the partial lists merged. The lists are ordered by
+// FP64 FMAs, each warp 8 rows x 128 columns) and folds them from registers
+// straight into per-row sorted lists of the k best (distance, column) pairs;
+// column ranges are split over CTAs to fill the GPU and the partial lists
+// merged. The lists are ordered by
 // distance, then by column index, so the selected set and its order do not
 // depend on the tile schedule or the split (ties go to the smaller index). The
 // median is a radix select over the n*k selected distances (the lower median,
@@ -39,7 +40,7 @@ constexpr int TM = 64;    // rows (points i) per CTA
 constexpr int TN = 128;   // columns (points j) per tile
 constexpr int DC = 32;    // dimension chunk staged in shared memory
 constexpr int NT = 256;   // threads per CTA: 16 x 16, 4 rows x 8 columns each
-constexpr int SA = TM + 4, SBW = TN + 4, SD = TN + 4;  // padded row strides (16-byte multiples)
+constexpr int SA = TM + 4, SBW = TN + 4;  // padded row strides (16-byte multiples)
 constexpr int kMaxSplit = 8;
 constexpr int kMaxK = 256;
 
@@ -102,7 +103,82 @@ __device__ __forceinline__ void list_insert(T* Lv, int* Li, int K, T cv, int cj,
 
 template <class T>
 size_t knn_smem_bytes(int K) {
-  return ((size_t)DC * SA + (size_t)DC * SBW + (size_t)TM * SD + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
+  return ((size_t)DC * SA + (size_t)DC * SBW + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
+}
+
+// Stage one DC-wide chunk of the points [base, base + rows) (rows < lim are
+// real, the rest zero) into s[kk][row] (row stride S). With `vec` the rows are
+// read as 16-byte vectors along the dimension (dim a multiple of the vector
+// width, 16-byte aligned rows), else element by element.
+template <class T, int ROWS, int S>
+__device__ __forceinline__ void stage_chunk(T* __restrict__ s, const T* __restrict__ x, int base, int lim, int dim,
+                                            int k0, int kc, bool vec) {
+  constexpr int VW = 16 / (int)sizeof(T);
+  if (vec) {
+    constexpr int NV = DC / VW;
+    for (int e = threadIdx.x; e < ROWS * NV; e += NT) {
+      const int r = e / NV, kv = e % NV;
+      const int g = base + r;
+      T v[VW];
+      if (g < lim && kv * VW < kc) {
+        const T* src = x + (size_t)g * dim + k0 + kv * VW;
+        if constexpr (sizeof(T) == 4) {
+          const float4 a = *reinterpret_cast<const float4*>(src);
+          v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        } else {
+          const double2 a = *reinterpret_cast<const double2*>(src);
+          v[0] = a.x; v[1] = a.y;
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < VW; ++t) v[t] = T(0);
+      }
+#pragma unroll
+      for (int t = 0; t < VW; ++t) s[(kv * VW + t) * S + r] = v[t];
+    }
+  } else {
+    for (int e = threadIdx.x; e < ROWS * DC; e += NT) {
+      const int r = e / DC, kk = e % DC;
+      const int g = base + r;
+      s[kk * S + r] = (g < lim && kk < kc) ? x[(size_t)g * dim + k0 + kk] : T(0);
+    }
+  }
+}
+
+// Warp-wide bitonic sort of 128 (value, column) pairs, 4 per lane (element
+// 4 * lane + q), ascending in (value, column) order.
+template <class T>
+__device__ __forceinline__ void warp_sort128(T (&v)[4], int (&ix)[4], int lane) {
+#pragma unroll
+  for (int s = 2; s <= 128; s <<= 1) {
+#pragma unroll
+    for (int jj = s >> 1; jj > 0; jj >>= 1) {
+      if (jj >= 4) {
+        const int lm = jj >> 2;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const T pv = __shfl_xor_sync(0xffffffffu, v[q], lm);
+          const int pi = __shfl_xor_sync(0xffffffffu, ix[q], lm);
+          const int e = 4 * lane + q;
+          const bool keep_min = ((e & jj) == 0) == ((e & s) == 0);
+          const bool take = keep_min ? lexless(pv, pi, v[q], ix[q]) : lexless(v[q], ix[q], pv, pi);
+          if (take) { v[q] = pv; ix[q] = pi; }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (q & jj) continue;
+          const int q2 = q | jj;
+          const bool asc = ((4 * lane + q) & s) == 0;
+          const bool sw = asc ? lexless(v[q2], ix[q2], v[q], ix[q]) : lexless(v[q], ix[q], v[q2], ix[q2]);
+          if (sw) {
+            const T tv = v[q]; v[q] = v[q2]; v[q2] = tv;
+            const int ti = ix[q]; ix[q] = ix[q2]; ix[q2] = ti;
+          }
+        }
+      }
+    }
+  }
 }
 
 // Rows [i0, i0 + TM) against columns [c_begin, c_end): the K smallest
@@ -110,86 +186,116 @@ size_t knn_smem_bytes(int K) {
 // [(row * nsplit + split) * K]. dist = fma(-2, <x_i, x_j>, |x_j|^2 + |x_i|^2),
 // the reference's norm sum with the GEMM's -2 x^T x added
 // (src/laplacian_cuda_kernel.cu:25-43, 88-106).
+//
+// Warp w owns rows 8w .. 8w+7 of the block: per 128-column tile each lane
+// accumulates 8 rows x 4 columns (lane l: columns 4l .. 4l+3) from the shared
+// chunks and then folds its distances straight into the warp's lists (kept in
+// shared memory): the first tile of a split is sorted whole (when K <= 128),
+// later tiles insert only candidates that beat the current K-th entry.
 template <class T>
-__global__ void __launch_bounds__(NT) k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim,
-                                            int K, int cols_per_split, int nsplit, T* __restrict__ out_v,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1) k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim,
+                                            int K, int cols_per_split, int nsplit, bool vec, T* __restrict__ out_v,
                                             int* __restrict__ out_i) {
   extern __shared__ __align__(16) unsigned char lap_smem[];
   T* sA = reinterpret_cast<T*>(lap_smem);  // [DC][SA]: x_i chunk, transposed
   T* sB = sA + DC * SA;                     // [DC][SBW]: x_j chunk, transposed
-  T* sD = sB + DC * SBW;                    // [TM][SD]: one tile of distances
-  T* lv = sD + TM * SD;                     // [TM][K]: list values
+  T* lv = sB + DC * SBW;                    // [TM][K]: list values
   int* li = reinterpret_cast<int*>(lv + TM * K);  // [TM][K]: list columns
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int lane = tid & 31, warp = tid >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i0 = blockIdx.x * TM;
   const int split = blockIdx.y;
   const int c_begin = split * cols_per_split;
   const int c_end = min(n, c_begin + cols_per_split);
+  const int rw = warp * 8;  // first row of this warp within the block
   const T inf = T(INFINITY);
-  for (int e = tid; e < TM * K; e += NT) { lv[e] = inf; li[e] = INT_MAX; }
-  T ni[4];
+  for (int e = lane; e < 8 * K; e += 32) { lv[rw * K + e] = inf; li[rw * K + e] = INT_MAX; }
+  T ni[8];
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int r = i0 + ty * 4 + a;
+  for (int a = 0; a < 8; ++a) {
+    const int r = i0 + rw + a;
     ni[a] = r < n ? norm[r] : T(0);
   }
   for (int j0 = c_begin; j0 < c_end; j0 += TN) {
-    T acc[4][8];
+    T acc[8][4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < 8; ++a)
 #pragma unroll
-      for (int b = 0; b < 8; ++b) acc[a][b] = T(0);
+      for (int q = 0; q < 4; ++q) acc[a][q] = T(0);
     for (int k0 = 0; k0 < dim; k0 += DC) {
       const int kc = min(DC, dim - k0);
-      __syncthreads();  // the previous chunk and the previous tile's selection are done
-      for (int e = tid; e < TM * DC; e += NT) {
-        const int r = e / DC, kk = e % DC;
-        const int gi = i0 + r;
-        sA[kk * SA + r] = (gi < n && kk < kc) ? x[(size_t)gi * dim + k0 + kk] : T(0);
-      }
-      for (int e = tid; e < TN * DC; e += NT) {
-        const int c = e / DC, kk = e % DC;
-        const int gj = j0 + c;
-        sB[kk * SBW + c] = (gj < c_end && kk < kc) ? x[(size_t)gj * dim + k0 + kk] : T(0);
-      }
+      __syncthreads();  // every warp is done with the previous chunk
+      stage_chunk<T, TM, SA>(sA, x, i0, n, dim, k0, kc, vec);
+      stage_chunk<T, TN, SBW>(sB, x, j0, c_end, dim, k0, kc, vec);
       __syncthreads();
+#pragma unroll 4
       for (int kk = 0; kk < kc; ++kk) {
-        T av[4], bv[8];
-        ld4s<T>(sA + kk * SA + ty * 4, av);
-        ld4s<T>(sB + kk * SBW + tx * 4, bv);
-        ld4s<T>(sB + kk * SBW + 64 + tx * 4, bv + 4);
+        T av[8], bv[4];
+        ld4s<T>(sA + kk * SA + rw, av);
+        ld4s<T>(sA + kk * SA + rw + 4, av + 4);
+        ld4s<T>(sB + kk * SBW + 4 * lane, bv);
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 8; ++a)
 #pragma unroll
-          for (int b = 0; b < 8; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+          for (int q = 0; q < 4; ++q) acc[a][q] = fma(av[a], bv[q], acc[a][q]);
       }
     }
-    // distances of the tile; columns past the range are NaN, which no
-    // comparison selects
+    // distances; columns past the range are NaN (never selected)
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const int c = b < 4 ? tx * 4 + b : 64 + tx * 4 + (b - 4);
-      const int gj = j0 + c;
+    for (int q = 0; q < 4; ++q) {
+      const int gj = j0 + 4 * lane + q;
       const T nj = gj < c_end ? norm[gj] : T(0);
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
-        sD[(ty * 4 + a) * SD + c] = gj < c_end ? fma(T(-2), acc[a][b], nj + ni[a]) : T(NAN);
+      for (int a = 0; a < 8; ++a) acc[a][q] = gj < c_end ? fma(T(-2), acc[a][q], nj + ni[a]) : T(NAN);
     }
-    __syncthreads();
-    // selection: warp w owns rows 8w .. 8w+7 of the block for the whole kernel
-    for (int rr = 0; rr < TM / 8; ++rr) {
-      const int r = warp * (TM / 8) + rr;
-      if (i0 + r >= n) break;
-      T* Lv = lv + r * K;
-      int* Li = li + r * K;
+    const bool first = j0 == c_begin && K <= TN;
+    // rows with a candidate that beats their current K-th entry (all rows on
+    // a split's first tile, which is sorted whole)
+    unsigned todo = 0;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const T tv = lv[(rw + a) * K + K - 1];
+      const int ti = li[(rw + a) * K + K - 1];
+      bool any = first;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) any = any || lexless(acc[a][q], j0 + 4 * lane + q, tv, ti);
+      if (__ballot_sync(0xffffffffu, any) && i0 + rw + a < n) todo |= 1u << a;
+    }
+    // those rows one at a time (a rolled loop keeps the sort and insert code
+    // single)
+    while (todo) {
+      const int a = __ffs(todo) - 1;
+      todo &= todo - 1;
+      T d4[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        T r = acc[0][q];
+#pragma unroll
+        for (int b = 1; b < 8; ++b) r = a == b ? acc[b][q] : r;
+        d4[q] = r;
+      }
+      T* Lv = lv + (rw + a) * K;
+      int* Li = li + (rw + a) * K;
+      if (first) {
+        int ix[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const bool ok = d4[q] == d4[q];  // NaN (past the range) sorts last
+          ix[q] = ok ? j0 + 4 * lane + q : INT_MAX;
+          if (!ok) d4[q] = inf;
+        }
+        warp_sort128<T>(d4, ix, lane);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (4 * lane + q < K) { Lv[4 * lane + q] = d4[q]; Li[4 * lane + q] = ix[q]; }
+        __syncwarp();
+        continue;
+      }
       T tv = Lv[K - 1];
       int ti = Li[K - 1];
 #pragma unroll
-      for (int q = 0; q < TN / 32; ++q) {
-        const int c = q * 32 + lane;
-        const T dv = sD[r * SD + c];
-        const int j = j0 + c;
+      for (int q = 0; q < 4; ++q) {
+        const T dv = d4[q];
+        const int j = j0 + 4 * lane + q;
         bool pass = lexless(dv, j, tv, ti);
         unsigned m = __ballot_sync(0xffffffffu, pass);
         while (m) {
@@ -206,15 +312,15 @@ __global__ void __launch_bounds__(NT) k_knn(const T* __restrict__ x, const T* __
       }
     }
   }
-  __syncthreads();
-  for (int rr = 0; rr < TM / 8; ++rr) {
-    const int r = warp * (TM / 8) + rr;
-    const int gi = i0 + r;
+  __syncwarp();
+#pragma unroll 1
+  for (int a = 0; a < 8; ++a) {
+    const int gi = i0 + rw + a;
     if (gi >= n) break;
     const size_t o = ((size_t)gi * nsplit + split) * K;
     for (int e = lane; e < K; e += 32) {
-      out_v[o + e] = lv[r * K + e];
-      out_i[o + e] = li[r * K + e];
+      out_v[o + e] = lv[(rw + a) * K + e];
+      out_i[o + e] = li[(rw + a) * K + e];
     }
   }
 }
@@ -351,27 +457,24 @@ __global__ void k_lap_weights(const T* __restrict__ fv, const int* __restrict__ 
 }
 
 struct Layout {
-  int nsplit, cols_per_split;
+  int max_split;  // column splits the partial-list buffers hold
   size_t off_norm, off_pv, off_pi, off_fv, off_fi, off_state, off_med, total;
 };
 
 inline size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Workspace: norms, partial lists of up to max_split column splits (bounded to
+// 256 MiB), the merged lists, the select state and the median.
 inline Layout layout(int n, int k, size_t es) {
   Layout L{};
-  const int rowblocks = (n + TM - 1) / TM;
-  int ns = std::max(1, std::min(kMaxSplit, (2 * 152 + rowblocks - 1) / rowblocks));
-  int cps = (n + ns - 1) / ns;
-  cps = (cps + TN - 1) / TN * TN;
-  ns = (n + cps - 1) / cps;
-  L.nsplit = ns;
-  L.cols_per_split = cps;
+  const size_t nk = (size_t)n * k;
+  const size_t per_split = nk * (es + 4);
+  L.max_split = (int)std::max<size_t>(1, std::min<size_t>(kMaxSplit, ((size_t)256 << 20) / per_split));
   size_t off = 0;
   L.off_norm = off; off = al256(off + (size_t)n * es);
-  const size_t nk = (size_t)n * k;
-  if (ns > 1) {
-    L.off_pv = off; off = al256(off + nk * ns * es);
-    L.off_pi = off; off = al256(off + nk * ns * 4);
+  if (L.max_split > 1) {
+    L.off_pv = off; off = al256(off + nk * L.max_split * es);
+    L.off_pi = off; off = al256(off + nk * L.max_split * 4);
   }
   L.off_fv = off; off = al256(off + nk * es);
   L.off_fi = off; off = al256(off + nk * 4);
@@ -381,33 +484,67 @@ inline Layout layout(int n, int k, size_t es) {
   return L;
 }
 
+// Column splits: at least one full wave of CTAs where max_split allows (the
+// kernel needs every resident slot to hide its latencies), then the count that
+// minimises waves x CTA length, a CTA costing its tiles plus about two tiles of
+// list set-up. The result does not depend on the choice.
+inline int choose_split(int n, int max_split, int slots) {
+  const int rows = (n + TM - 1) / TM;
+  slots = std::max(1, slots);
+  int best = 0;
+  double best_cost = 0;
+  for (int pass = 0; pass < 2 && best == 0; ++pass) {
+    for (int ns = 1; ns <= max_split; ++ns) {
+      const int cps = ((n + ns - 1) / ns + TN - 1) / TN * TN;
+      if ((n + cps - 1) / cps != ns) continue;
+      if (pass == 0 && rows * ns < slots) continue;
+      const double waves = std::ceil((double)rows * ns / slots);
+      const double cost = waves * (cps / TN + 2);
+      if (best == 0 || cost < best_cost * 0.97) { best = ns; best_cost = cost; }
+    }
+  }
+  if (best == 0) {  // no split reaches a full wave: the most splits there are
+    for (int ns = max_split; ns >= 1 && best == 0; --ns) {
+      const int cps = ((n + ns - 1) / ns + TN - 1) / TN * TN;
+      if ((n + cps - 1) / cps == ns) best = ns;
+    }
+  }
+  return std::max(1, best);
+}
+
 template <class T>
 int run(const T* x, int n, int dim, int k, long long* ind, float* val, unsigned char* ws, cudaStream_t st) {
   const Layout L = layout(n, k, sizeof(T));
   T* norm = reinterpret_cast<T*>(ws + L.off_norm);
   T* fv = reinterpret_cast<T*>(ws + L.off_fv);
   int* fi = reinterpret_cast<int*>(ws + L.off_fi);
-  T* pv = L.nsplit > 1 ? reinterpret_cast<T*>(ws + L.off_pv) : fv;
-  int* pi = L.nsplit > 1 ? reinterpret_cast<int*>(ws + L.off_pi) : fi;
   SelectState* sel = reinterpret_cast<SelectState*>(ws + L.off_state);
   T* med = reinterpret_cast<T*>(ws + L.off_med);
   const size_t smem = knn_smem_bytes<T>(k);
-  int dev = 0, optin = 0;
+  int dev = 0, optin = 0, sms = 0, occ = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian: ") + cudaGetErrorString(e));
   if (smem > (size_t)optin)
     return fail(CTGB_ERR_INVALID, "laplacian: k too large for this dtype (" + std::to_string(smem) +
                                       " bytes of shared memory per CTA needed)");
   e = cudaFuncSetAttribute(k_knn<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_knn<T>, NT, smem);
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian smem: ") + cudaGetErrorString(e));
+  const int ns = choose_split(n, L.max_split, sms * std::max(1, occ));
+  const int cps = ((n + ns - 1) / ns + TN - 1) / TN * TN;
+  T* pv = ns > 1 ? reinterpret_cast<T*>(ws + L.off_pv) : fv;
+  int* pi = ns > 1 ? reinterpret_cast<int*>(ws + L.off_pi) : fi;
+  constexpr int VW = 16 / (int)sizeof(T);
+  const bool vec = dim % VW == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
   k_sqnorm<T><<<(n + 255) / 256, 256, 0, st>>>(x, n, dim, norm);
-  dim3 grid((n + TM - 1) / TM, L.nsplit);
-  k_knn<T><<<grid, NT, smem, st>>>(x, norm, n, dim, k, L.cols_per_split, L.nsplit, pv, pi);
-  if (L.nsplit > 1) k_knn_merge<T><<<(n + 127) / 128, 128, 0, st>>>(pv, pi, n, L.nsplit, k, fv, fi);
+  dim3 grid((n + TM - 1) / TM, ns);
+  k_knn<T><<<grid, NT, smem, st>>>(x, norm, n, dim, k, cps, ns, vec, pv, pi);
+  if (ns > 1) k_knn_merge<T><<<(n + 127) / 128, 128, 0, st>>>(pv, pi, n, ns, k, fv, fi);
   const size_t m = (size_t)n * k;
   k_select_init<<<1, 256, 0, st>>>(sel, (m - 1) / 2);
-  const int sb = (int)std::max<size_t>(1, std::min<size_t>((m + 2047) / 2048, 152 * 4));
+  const int sb = (int)std::max<size_t>(1, std::min<size_t>((m + 2047) / 2048, (size_t)sms * 4));
   for (int p = Key<T>::kPasses - 1; p >= 0; --p) k_select_pass<T><<<sb, 256, 0, st>>>(fv, m, 8 * p, sel, med);
   k_lap_weights<T><<<(n + 127) / 128, 128, 0, st>>>(fv, fi, n, k, med, ind, val);
   e = cudaGetLastError();
