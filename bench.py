@@ -184,6 +184,21 @@ def run_reference(args):
     return 0
 
 
+LAPLACIAN_CASE = {"points": 16384, "dim": 64, "k": 16}
+
+
+def _laplacian_timing(fn, timed, dev):
+    """Mean time of one laplacian call (fp32 Gaussian points, seed 1) with its
+    FP32 FMA count n^2 * dim."""
+    import torch
+    c = LAPLACIAN_CASE
+    x = torch.from_numpy(np.random.default_rng(1).standard_normal((c["points"], c["dim"])).astype(np.float32)).to(dev)
+    ms = timed(lambda: fn(x, c["k"]))
+    fma = float(c["points"]) ** 2 * c["dim"]
+    return {"case": dict(c), "ms": ms, "fma_per_s": fma / (ms / 1e3),
+            "note": "kNN graph adjacency of n points: distances, top-k, median, weights, COO output"}
+
+
 def _reference_cuda(w, args):
     """The reference's own CUDA kernels (src/fan_ed_kernel.cu prj_fan_ed and
     prj_t_fan_ed, compiled unchanged for sm_103a, oracle/ref_cuda.py) on the full
@@ -239,13 +254,29 @@ def _reference_cuda(w, args):
         torch.cuda.synchronize()
         e2e.append(a.elapsed_time(b))
     e2e_ms = statistics.mean(e2e)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    lap = _laplacian_timing(lambda x, k: ref.laplacian(x, k), timed, dev) if ref_cuda.laplacian_available() else None
     return {"value": ru / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
             "ms_projection": statistics.mean(t_a), "ms_projection_t": statistics.mean(t_at),
             "e2e": {"value": ru / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": img_h.numel() * 4, "d2h_bytes_per_step": img_h.numel() * 4},
             "kind": "reference CUDA kernels (src/fan_ed_kernel.cu) compiled for sm_103a, launched with the "
                     "reference wrappers' grids and output allocations",
-            "dtype": "f32", "gpu_launches_per_step": 2}
+            "dtype": "f32", "gpu_launches_per_step": 2, "laplacian": lap}
 
 
 def _fp32_peak(device) -> dict:
@@ -404,6 +435,9 @@ def run_ours(args):
     grad_fused = timed(lambda: data_gradient(img, y_meas, opts))
     grad_composed = timed(lambda: ctlib.projection_t(ctlib.projection(img, opts) - y_meas, opts))
 
+    # -- kNN graph adjacency (laplacian) on its own synthetic points ----------
+    lap = _laplacian_timing(lambda x, k: ctlib.laplacian(x, k), timed, dev)
+
     # -- parity of the timed operator pair vs the FP64 oracle (1 slice) -------
     parity = None
     if rank == 0:
@@ -463,6 +497,7 @@ def run_ours(args):
                 "data_gradient": {"ms_fused": grad_fused, "ms_composed": grad_composed,
                                   "note": "A^T(Ax - y) for the same batch: ctgb_data_gradient vs projection, "
                                           "subtraction, projection_t"},
+                "laplacian": lap,
                 "gpu_launches": 4 * args.steps,
                 "clocks": clocks, "roofline": roof, "roofline_fp32": roof_fp32, "parity": parity,
                 "cpu_baseline": cb}
