@@ -199,6 +199,31 @@ def _laplacian_timing(fn, timed, dev):
             "note": "kNN graph adjacency of n points: distances, top-k, median, weights, COO output"}
 
 
+def run_laplacian_only(args):
+    """One JSON line with the laplacian case alone (W warm-up, K timed calls)."""
+    import torch
+    import ctlib_gb300 as ctlib
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    print(json.dumps({"only_laplacian": True, **_laplacian_timing(lambda x, k: ctlib.laplacian(x, k), timed, dev)}),
+          flush=True)
+    return 0
+
+
 def _reference_cuda(w, args):
     """The reference's own CUDA kernels (src/fan_ed_kernel.cu prj_fan_ed and
     prj_t_fan_ed, compiled unchanged for sm_103a, oracle/ref_cuda.py) on the full
@@ -638,9 +663,13 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch schedules")
     ap.add_argument("--only-step", action="store_true",
                     help="time only the batched projection + projection_t step (for profiler runs)")
+    ap.add_argument("--only-laplacian", action="store_true",
+                    help="time only the laplacian case (16384 points, dimension 64, k = 16; for profiler runs)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
+    if args.only_laplacian:
+        return run_laplacian_only(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload.startswith("ragged"):

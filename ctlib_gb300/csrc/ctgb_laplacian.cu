@@ -75,9 +75,24 @@ __global__ void k_sqnorm(const T* __restrict__ x, int n, int dim, T* __restrict_
 
 // Insert (cv, cj) into the sorted list (Lv, Li) of K entries, dropping the
 // last one; the whole warp takes part. The caller guarantees that (cv, cj)
-// precedes the last entry.
+// precedes the last entry. Lists of up to 32 entries are shifted through
+// registers (lane e holds entry e), longer ones chunk by chunk in shared memory.
 template <class T>
 __device__ __forceinline__ void list_insert(T* Lv, int* Li, int K, T cv, int cj, int lane) {
+  if (K <= 32) {
+    const bool in = lane < K;
+    T v = in ? Lv[lane] : T(0);
+    int ix = in ? Li[lane] : INT_MAX;
+    const int p = __popc(__ballot_sync(0xffffffffu, in && lexless(v, ix, cv, cj)));
+    const T uv = __shfl_up_sync(0xffffffffu, v, 1);
+    const int ui = __shfl_up_sync(0xffffffffu, ix, 1);
+    if (lane == p) { v = cv; ix = cj; }
+    else if (lane > p) { v = uv; ix = ui; }
+    __syncwarp();
+    if (in) { Lv[lane] = v; Li[lane] = ix; }
+    __syncwarp();
+    return;
+  }
   int p = 0;
   for (int e0 = 0; e0 < K; e0 += 32) {
     const int e = e0 + lane;
@@ -403,9 +418,18 @@ __global__ void __launch_bounds__(256) k_select_pass(const T* __restrict__ v, si
   for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
   __syncthreads();
   const U prefix = (U)st->prefix, mask = (U)st->mask;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < m; e += (size_t)gridDim.x * blockDim.x) {
-    const U key = Key<T>::enc(v[e]);
-    if ((key & mask) == prefix) atomicAdd(&h[(unsigned)(key >> shift) & 255u], 1u);
+  // the values share most leading digits, so the lanes of a warp that hit the
+  // same bin add once, through their leader
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t m_round = (m + 31) / 32 * 32;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < m_round; e += stride) {
+    unsigned bin = 256u;  // no bin
+    if (e < m) {
+      const U key = Key<T>::enc(v[e]);
+      if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, bin);
+    if (bin < 256u && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1)) atomicAdd(&h[bin], (unsigned)__popc(same));
   }
   __syncthreads();
   for (int b = threadIdx.x; b < 256; b += blockDim.x)
