@@ -116,9 +116,14 @@ __device__ __forceinline__ void list_insert(T* Lv, int* Li, int K, T cv, int cj,
   __syncwarp();
 }
 
+// lists of up to kStageK entries leave room for a per-warp staging area of the
+// tile's distances at three CTAs per SM
+constexpr int kStageK = 32;
+
 template <class T>
 size_t knn_smem_bytes(int K) {
-  return ((size_t)DC * SA + (size_t)DC * SBW + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
+  const size_t stage = K <= kStageK ? (size_t)TM * TN : 0;
+  return ((size_t)DC * SA + (size_t)DC * SBW + stage + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
 }
 
 // Stage one DC-wide chunk of the points [base, base + rows) (rows < lim are
@@ -214,7 +219,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1) k_knn(const T* __r
   extern __shared__ __align__(16) unsigned char lap_smem[];
   T* sA = reinterpret_cast<T*>(lap_smem);  // [DC][SA]: x_i chunk, transposed
   T* sB = sA + DC * SA;                     // [DC][SBW]: x_j chunk, transposed
-  T* lv = sB + DC * SBW;                    // [TM][K]: list values
+  const bool staged = K <= kStageK;
+  T* sD = sB + DC * SBW;                    // [TM][TN] if staged: the tile's distances, for per-row work
+  T* lv = sD + (staged ? TM * TN : 0);      // [TM][K]: list values
   int* li = reinterpret_cast<int*>(lv + TM * K);  // [TM][K]: list columns
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i0 = blockIdx.x * TM;
@@ -276,17 +283,34 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1) k_knn(const T* __r
       if (__ballot_sync(0xffffffffu, any) && i0 + rw + a < n) todo |= 1u << a;
     }
     // those rows one at a time (a rolled loop keeps the sort and insert code
-    // single)
+    // single), reading their distances back from the warp's staging area
+    T* wD = sD + rw * TN;
+    if (todo && staged) {
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        if constexpr (sizeof(T) == 4) {
+          *reinterpret_cast<float4*>(wD + a * TN + 4 * lane) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+        } else {
+          reinterpret_cast<double2*>(wD + a * TN + 4 * lane)[0] = make_double2(acc[a][0], acc[a][1]);
+          reinterpret_cast<double2*>(wD + a * TN + 4 * lane)[1] = make_double2(acc[a][2], acc[a][3]);
+        }
+      }
+      __syncwarp();
+    }
     while (todo) {
       const int a = __ffs(todo) - 1;
       todo &= todo - 1;
       T d4[4];
+      if (staged) {
+        ld4s<T>(wD + a * TN + 4 * lane, d4);
+      } else {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        T r = acc[0][q];
+        for (int q = 0; q < 4; ++q) {
+          T r = acc[0][q];
 #pragma unroll
-        for (int b = 1; b < 8; ++b) r = a == b ? acc[b][q] : r;
-        d4[q] = r;
+          for (int b = 1; b < 8; ++b) r = a == b ? acc[b][q] : r;
+          d4[q] = r;
+        }
       }
       T* Lv = lv + (rw + a) * K;
       int* Li = li + (rw + a) * K;
@@ -407,8 +431,9 @@ __global__ void k_select_init(SelectState* st, unsigned long long rank) {
 
 // One 8-bit digit (most significant first) of the radix select of the value of
 // rank st->rank among v[0, m). Every CTA histograms the digit of the values
-// that match the digits found so far; the last CTA to finish (ticket) picks the
-// digit, resets the histogram, and after the last digit writes the value.
+// that match the digits found so far; the last CTA to finish (ticket) reads
+// and clears the histogram, picks the digit, and after the last digit writes
+// the value.
 template <class T>
 __global__ void __launch_bounds__(256) k_select_pass(const T* __restrict__ v, size_t m, int shift, SelectState* st,
                                                      T* __restrict__ out) {
@@ -438,21 +463,23 @@ __global__ void __launch_bounds__(256) k_select_pass(const T* __restrict__ v, si
   __syncthreads();
   if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
+  // the last CTA: read (and clear) the global histogram together, then one
+  // thread picks the digit
   __threadfence();
-  volatile unsigned int* hist = st->hist;
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = atomicExch(&st->hist[b], 0u);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   unsigned long long rank = st->rank;
   int b = 0;
   for (; b < 255; ++b) {
-    const unsigned int c = hist[b];
-    if (rank < c) break;
-    rank -= c;
+    if (rank < h[b]) break;
+    rank -= h[b];
   }
   const U np = prefix | ((U)b << shift);
   st->prefix = np;
   st->mask = mask | ((U)255 << shift);
   st->rank = rank;
-  for (int i = 0; i < 256; ++i) hist[i] = 0;
   st->ticket = 0;
   if (shift == 0) *out = Key<T>::dec(np);
 }
