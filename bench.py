@@ -501,7 +501,9 @@ def run_ours(args):
                      "measured_fp32": peak}
 
     if rank == 0:
-        cb = _cpu_baseline(w)
+        # the CPU baseline is timed at N = 1 only (a replica run would only add
+        # the same host measurement to every line)
+        cb = _cpu_baseline(w) if ws == 1 else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic ellipse phantoms (seeded)",
