@@ -211,11 +211,12 @@ __device__ __forceinline__ void warp_sort128(T (&v)[4], int (&ix)[4], int lane) 
 // accumulates 8 rows x 4 columns (lane l: columns 4l .. 4l+3) from the shared
 // chunks and then folds its distances straight into the warp's lists (kept in
 // shared memory): the first tile of a split is sorted whole (when K <= 128),
-// later tiles insert only candidates that beat the current K-th entry.
+// later tiles insert only candidates that beat the current K-th entry. Three
+// CTAs per SM for fp32 (80 registers); fp64 needs more registers and runs one.
 template <class T>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1) k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim,
-                                            int K, int cols_per_split, int nsplit, bool vec, T* __restrict__ out_v,
-                                            int* __restrict__ out_i) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
+    k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim, int K, int cols_per_split, int nsplit,
+          bool vec, T* __restrict__ out_v, int* __restrict__ out_i) {
   extern __shared__ __align__(16) unsigned char lap_smem[];
   T* sA = reinterpret_cast<T*>(lap_smem);  // [DC][SA]: x_i chunk, transposed
   T* sB = sA + DC * SA;                     // [DC][SBW]: x_j chunk, transposed
