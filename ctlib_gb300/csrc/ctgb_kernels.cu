@@ -174,8 +174,8 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 // the pair is touched once per kFoldEvery lines / views, so it need not hold
 // registers; layout [2][SB][blockDim] keeps the accesses conflict-free.
 template <class T, int SB>
-__device__ __forceinline__ void kahan_fold_smem(T* acc, T (&blk)[SB]) {
-  const int nt = blockDim.x, t = threadIdx.x;
+__device__ __forceinline__ void kahan_fold_smem(T* acc, T (&blk)[SB], int nt) {
+  const int t = threadIdx.x;
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     T* sum = acc + (size_t)s * nt + t;
@@ -189,9 +189,9 @@ __device__ __forceinline__ void kahan_fold_smem(T* acc, T (&blk)[SB]) {
 }
 
 template <class T, int SB>
-__device__ __forceinline__ void kahan_init_smem(T* acc) {
+__device__ __forceinline__ void kahan_init_smem(T* acc, int nt) {
 #pragma unroll
-  for (int s = 0; s < 2 * SB; ++s) acc[(size_t)s * blockDim.x + threadIdx.x] = T(0);
+  for (int s = 0; s < 2 * SB; ++s) acc[(size_t)s * nt + threadIdx.x] = T(0);
 }
 
 // Kahan fold of a block partial into (sum, comp); the partial is reset.
@@ -379,7 +379,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
 
   extern __shared__ unsigned char det_smem[];
   T* acc = reinterpret_cast<T*>(det_smem);  // [2][SB][blockDim]: running sum, compensation
-  kahan_init_smem<T, SB>(acc);
+  kahan_init_smem<T, SB>(acc, blockDim.x);
   T blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) blk[s] = T(0);
@@ -409,7 +409,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       k = 0;
     }
     if (k >= N || b <= T(0)) {
-      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
+      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
       continue;
     }
     // pixels past the line's end take no weight: with b clamped to N - k their
@@ -470,9 +470,9 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(w, u[i], blk[qd * QW + i]);
       }
     }
-    if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk);
+    if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
   }
-  kahan_fold_smem<T, SB>(acc, blk);
+  kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
   T fac = T(1);
   if (KIND == kA) fac = P.fq[(size_t)v * P.D + d];
   else if (P.scan == kFanEA) fac = P.fbt[(size_t)v * P.D + d];
@@ -799,7 +799,7 @@ __host__ __device__ __forceinline__ int view_split(int views) { return views >= 
 // a pixel can reach (including the seed correction and the step back when the
 // offset is negative) lies inside it.
 constexpr int kWin = 64;   // cells per staged view window (multiple of 4)
-constexpr int kSlots = 6;  // views in flight per CTA
+constexpr int kSlots = 7;  // views in flight per CTA
 
 template <class T, int SB>
 struct PixSlot {
@@ -833,8 +833,9 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   extern __shared__ __align__(16) unsigned char pix_smem[];
   const int R = (int)(blockDim.x >> 5) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][blockDim]: running sum, compensation
-  unsigned char* slots = pix_smem + (size_t)2 * SB * blockDim.x * sizeof(T);
+  const int CT = 32 * R;                     // consumer threads
+  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][CT]: running sum, compensation
+  unsigned char* slots = pix_smem + (size_t)2 * SB * CT * sizeof(T);
   const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R;
   const int part = blockIdx.z % nsplit, g = blockIdx.z / nsplit;
   const int V = P.V, D = P.D, Dp = P.Dp;
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   const bool active = c < P.W && r < P.H;
   const T pcx = active ? P.colc[c] : T(0);
   const T pcy = active ? P.rowc[r] : T(0);
-  kahan_init_smem<T, SB>(acc);
+  kahan_init_smem<T, SB>(acc, CT);
   T blk[SB];
 #pragma unroll
   for (int s = 0; s < SB; ++s) blk[s] = T(0);
@@ -1018,17 +1019,17 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         }
       }
     } else if ((u % kFoldEvery) == kFoldEvery - 1) {
-      kahan_fold_smem<T, SB>(acc, blk);
+      kahan_fold_smem<T, SB>(acc, blk, CT);
     }
   }
   if (SV) return;
-  kahan_fold_smem<T, SB>(acc, blk);
+  kahan_fold_smem<T, SB>(acc, blk, CT);
   if (!active) return;
 #pragma unroll
   for (int s = 0; s < SB; ++s) {
     const int bb = g * SB + s;
     if (bb >= B) continue;
-    const T val = acc[(size_t)s * blockDim.x + threadIdx.x] * out_mul / out_div;
+    const T val = acc[(size_t)s * CT + threadIdx.x] * out_mul / out_div;
     T* dst = img + ((size_t)bb * P.H + r) * P.W + c;
     if (nsplit == 1) *dst = val;
     else atomicAdd(dst, val);
@@ -1050,13 +1051,13 @@ __device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int 
   T out = T(0);
   for (int part = 0; part < nsplit; ++part) {
     const int vbeg = (int)((long long)P.V * part / nsplit), vend = (int)((long long)P.V * (part + 1) / nsplit);
-    kahan_init_smem<T, 1>(acc);
+    kahan_init_smem<T, 1>(acc, blockDim.x);
     T blk[1] = {T(0)};
     for (int v = vbeg; v < vend; ++v) {
       pix_view_global<T, 1, KIND, 3>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
-      if (((v - vbeg) % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk);
+      if (((v - vbeg) % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk, blockDim.x);
     }
-    kahan_fold_smem<T, 1>(acc, blk);
+    kahan_fold_smem<T, 1>(acc, blk, blockDim.x);
     out += acc[threadIdx.x] * out_mul / out_div;
   }
   img[(size_t)r * P.W + c] = out;
@@ -1416,7 +1417,7 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   const int wpc = p->warps[sched];  // consumer warps (one pixel row each) + one producer warp
   dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
   const int nt = 32 * (wpc + 1);
-  const size_t smem = (size_t)2 * SB * nt * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
+  const size_t smem = (size_t)2 * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
   auto launch = [&](auto kern, T mul, T div) -> int {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
