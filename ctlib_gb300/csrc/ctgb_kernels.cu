@@ -172,7 +172,8 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 
 // Kahan fold of a block partial into a (sum, comp) pair kept in shared memory:
 // the pair is touched once per kFoldEvery lines / views, so it need not hold
-// registers; layout [2][SB][blockDim] keeps the accesses conflict-free.
+// registers; layout [2][SB][nt] (nt threads adding) keeps the accesses
+// conflict-free. The partial is reset.
 template <class T, int SB>
 __device__ __forceinline__ void kahan_fold_smem(T* acc, T (&blk)[SB], int nt) {
   const int t = threadIdx.x;
@@ -192,19 +193,6 @@ template <class T, int SB>
 __device__ __forceinline__ void kahan_init_smem(T* acc, int nt) {
 #pragma unroll
   for (int s = 0; s < 2 * SB; ++s) acc[(size_t)s * nt + threadIdx.x] = T(0);
-}
-
-// Kahan fold of a block partial into (sum, comp); the partial is reset.
-template <class T, int SB>
-__device__ __forceinline__ void kahan_fold(T (&sum)[SB], T (&comp)[SB], T (&blk)[SB]) {
-#pragma unroll
-  for (int s = 0; s < SB; ++s) {
-    const T y = sub_rn(blk[s], comp[s]);
-    const T t = add_rn(sum[s], y);
-    comp[s] = sub_rn(sub_rn(t, sum[s]), y);
-    sum[s] = t;
-    blk[s] = T(0);
-  }
 }
 
 enum Kind { kA = 0, kBt = 1, kAt = 2, kB = 3 };
