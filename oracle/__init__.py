@@ -129,10 +129,15 @@ def max_threads() -> int:
     return int(_load_oracle().oracle_max_threads())
 
 
+# operator numbers of the reference driver (oracle/ref_emu/ref_driver.inc)
+REF_OPS = {"projection": 0, "projection_t": 1, "backprojection": 2, "backprojection_t": 3, "backprojection_sv": 5}
+
+
 def ref_run(op, x: np.ndarray, opts, dtype=np.float32) -> np.ndarray:
-    """Run the reference's own kernel (CPU execution); ops 0-3 and 5 (single view)."""
+    """Run the reference's own kernel (CPU execution); ops 0-3 and 5 (single
+    view), by driver number or by name."""
     if isinstance(op, str):
-        op = OP_NAMES[op]
+        op = REF_OPS[op]
     lib = _load_ref()
     xin = np.ascontiguousarray(x, dtype=dtype)
     batch = xin.shape[0]
