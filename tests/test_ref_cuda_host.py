@@ -47,3 +47,4 @@ def test_no_gpu_no_module():
         pytest.skip("has a GPU")
     with pytest.raises(RuntimeError):
         ref_cuda.RefCuda()
+
