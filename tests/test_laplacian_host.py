@@ -1,6 +1,8 @@
 """Host-side contract of the laplacian's C ABI (ctgb_laplacian,
 ctgb_laplacian_workspace_size): workspace sizing and the arguments rejected
 before any device work. Needs the built library, no GPU."""
+
+
 def test_laplacian_workspace_contract():
     """ctgb_laplacian_workspace_size: 0 for invalid arguments, grows with n and k,
     256-byte multiples; bounded partial-list buffers."""
