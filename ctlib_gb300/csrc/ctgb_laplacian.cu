@@ -126,6 +126,37 @@ size_t knn_smem_bytes(int K) {
   return ((size_t)DC * SA + (size_t)DC * SBW + stage + (size_t)TM * K) * sizeof(T) + (size_t)TM * K * 4;
 }
 
+// ordered unsigned keys of floating-point values (sign-magnitude flipped)
+template <class T>
+struct Key;
+template <>
+struct Key<float> {
+  using U = unsigned int;
+  static constexpr int kPasses = 4;
+  __device__ static U enc(float v) {
+    const U u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  }
+  __device__ static float dec(U k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
+};
+template <>
+struct Key<double> {
+  using U = unsigned long long;
+  static constexpr int kPasses = 8;
+  __device__ static U enc(double v) {
+    const U u = (U)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | (1ull << 63));
+  }
+  __device__ static double dec(U k) { return __longlong_as_double((long long)((k >> 63) ? (k & ~(1ull << 63)) : ~k)); }
+};
+
+// lowers a row's shared bound to v (an fp32 K-th distance; NaN or +inf leave it)
+template <class T>
+__device__ __forceinline__ void publish_bound(unsigned* b, T v) {
+  const float f = (float)v;
+  if (f < INFINITY) atomicMin(b, Key<float>::enc(f));
+}
+
 // Stage one DC-wide chunk of the points [base, base + rows) (rows < lim are
 // real, the rest zero) into s[kk][row] (row stride S). With `vec` the rows are
 // read as 16-byte vectors along the dimension (dim a multiple of the vector
@@ -216,7 +247,7 @@ __device__ __forceinline__ void warp_sort128(T (&v)[4], int (&ix)[4], int lane) 
 template <class T>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
     k_knn(const T* __restrict__ x, const T* __restrict__ norm, int n, int dim, int K, int cols_per_split, int nsplit,
-          bool vec, T* __restrict__ out_v, int* __restrict__ out_i) {
+          bool vec, T* __restrict__ out_v, int* __restrict__ out_i, unsigned* __restrict__ gbound) {
   extern __shared__ __align__(16) unsigned char lap_smem[];
   T* sA = reinterpret_cast<T*>(lap_smem);  // [DC][SA]: x_i chunk, transposed
   T* sB = sA + DC * SA;                     // [DC][SBW]: x_j chunk, transposed
@@ -271,6 +302,19 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
       for (int a = 0; a < 8; ++a) acc[a][q] = gj < c_end ? fma(T(-2), acc[a][q], nj + ni[a]) : T(NAN);
     }
     const bool first = j0 == c_begin && K <= TN;
+    // the other column ranges' bounds: a candidate farther than some range's
+    // current K-th distance for the row cannot be among the row's K nearest
+    // (fp32 with several ranges; otherwise no bound)
+    if (gbound != nullptr && !first) {
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int r = i0 + rw + a;
+        const T bound = r < n ? (T)Key<float>::dec(gbound[r]) : T(INFINITY);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (acc[a][q] > bound) acc[a][q] = T(NAN);  // never selected
+      }
+    }
     // rows with a candidate that beats their current K-th entry (all rows on
     // a split's first tile, which is sorted whole)
     unsigned todo = 0;
@@ -328,6 +372,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
         for (int q = 0; q < 4; ++q)
           if (4 * lane + q < K) { Lv[4 * lane + q] = d4[q]; Li[4 * lane + q] = ix[q]; }
         __syncwarp();
+        if (gbound != nullptr && lane == 0) publish_bound(gbound + i0 + rw + a, Lv[K - 1]);
         continue;
       }
       T tv = Lv[K - 1];
@@ -350,6 +395,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
           m = __ballot_sync(0xffffffffu, pass);
         }
       }
+      if (gbound != nullptr && lane == 0) publish_bound(gbound + i0 + rw + a, tv);
     }
   }
   __syncwarp();
@@ -394,30 +440,6 @@ __global__ void k_knn_merge(const T* __restrict__ pv, const int* __restrict__ pi
     fi[(size_t)i * K + e] = bi;
   }
 }
-
-// ordered unsigned keys of floating-point values (sign-magnitude flipped)
-template <class T>
-struct Key;
-template <>
-struct Key<float> {
-  using U = unsigned int;
-  static constexpr int kPasses = 4;
-  __device__ static U enc(float v) {
-    const U u = __float_as_uint(v);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-  }
-  __device__ static float dec(U k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
-};
-template <>
-struct Key<double> {
-  using U = unsigned long long;
-  static constexpr int kPasses = 8;
-  __device__ static U enc(double v) {
-    const U u = (U)__double_as_longlong(v);
-    return (u >> 63) ? ~u : (u | (1ull << 63));
-  }
-  __device__ static double dec(U k) { return __longlong_as_double((long long)((k >> 63) ? (k & ~(1ull << 63)) : ~k)); }
-};
 
 struct SelectState {
   unsigned long long prefix, mask, rank;
@@ -510,7 +532,7 @@ __global__ void k_lap_weights(const T* __restrict__ fv, const int* __restrict__ 
 
 struct Layout {
   int max_split;  // column splits the partial-list buffers hold
-  size_t off_norm, off_pv, off_pi, off_fv, off_fi, off_state, off_med, total;
+  size_t off_norm, off_pv, off_pi, off_fv, off_fi, off_state, off_med, off_bound, total;
 };
 
 inline size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -532,6 +554,7 @@ inline Layout layout(int n, int k, size_t es) {
   L.off_fi = off; off = al256(off + nk * 4);
   L.off_state = off; off = al256(off + sizeof(SelectState));
   L.off_med = off; off = al256(off + es);
+  L.off_bound = off; off = al256(off + (size_t)n * 4);
   L.total = off;
   return L;
 }
@@ -592,7 +615,14 @@ int run(const T* x, int n, int dim, int k, long long* ind, float* val, unsigned 
   const bool vec = dim % VW == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
   k_sqnorm<T><<<(n + 255) / 256, 256, 0, st>>>(x, n, dim, norm);
   dim3 grid((n + TM - 1) / TM, ns);
-  k_knn<T><<<grid, NT, smem, st>>>(x, norm, n, dim, k, cps, ns, vec, pv, pi);
+  // shared per-row bounds between the column ranges (fp32): start at "none"
+  unsigned* gbound = nullptr;
+  if (sizeof(T) == 4 && ns > 1) {
+    gbound = reinterpret_cast<unsigned*>(ws + L.off_bound);
+    e = cudaMemsetAsync(gbound, 0xFF, (size_t)n * 4, st);
+    if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("laplacian bounds: ") + cudaGetErrorString(e));
+  }
+  k_knn<T><<<grid, NT, smem, st>>>(x, norm, n, dim, k, cps, ns, vec, pv, pi, gbound);
   if (ns > 1) k_knn_merge<T><<<(n + 127) / 128, 128, 0, st>>>(pv, pi, n, ns, k, fv, fi);
   const size_t m = (size_t)n * k;
   k_select_init<<<1, 256, 0, st>>>(sel, (m - 1) / 2);
