@@ -172,3 +172,13 @@ def test_laplacian_vs_reference_gpu(ct, ref, n, dim, k, dtype):
     vr = _by_column(cr, Wr._values().cpu().numpy().reshape(n, k))[~ties]
     v = _by_column(co, W._values().cpu().numpy().reshape(n, k))[~ties]
     assert np.linalg.norm(v - vr) <= 1e-5 * np.linalg.norm(vr)
+
+
+def test_fp64_large_k_fits_or_is_refused(ct):
+    """fp64 lists of many neighbours outgrow a CTA's shared memory: the call is
+    refused with a clear error instead of launching; a k that fits runs."""
+    x64 = torch.from_numpy(_points(400, 8, 13, np.float64)).cuda()
+    with pytest.raises(ValueError, match="shared memory"):
+        ct.laplacian(x64, 256)
+    W = ct.laplacian(x64, 64)
+    _check_vs_oracle(W, x64.cpu().numpy(), 64)
