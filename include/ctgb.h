@@ -209,8 +209,9 @@ int ctgb_wait_timeouts(int device, unsigned long long* count, int reset);
  * and normalised to sum 1 per row. Output, the reference's COO layout:
  * indices[0][i*k + e] = i, indices[1][i*k + e] = j_e (int64, 2 x n*k) and
  * values[i*k + e] (float32 for either dtype, as the reference's sparse tensor),
- * neighbours in increasing distance. 1 <= k <= min(n, 256); runs on the
- * current device. The n x n distance matrix is never formed. */
+ * neighbours in increasing distance. 1 <= k <= min(n, 256), and for fp64 at
+ * most what fits a CTA's shared memory (about 140; CTGB_ERR_INVALID beyond);
+ * runs on the current device. The n x n distance matrix is never formed. */
 size_t ctgb_laplacian_workspace_size(int n, int dim, int k, int dtype);
 int ctgb_laplacian(const void* points, int n, int dim, int k, int dtype, long long* indices, float* values,
                    void* workspace, size_t workspace_bytes, void* stream);
