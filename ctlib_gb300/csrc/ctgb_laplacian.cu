@@ -302,30 +302,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
       for (int a = 0; a < 8; ++a) acc[a][q] = gj < c_end ? fma(T(-2), acc[a][q], nj + ni[a]) : T(NAN);
     }
     const bool first = j0 == c_begin && K <= TN;
-    // the other column ranges' bounds: a candidate farther than some range's
-    // current K-th distance for the row cannot be among the row's K nearest
-    // (fp32 with several ranges; otherwise no bound)
-    if (gbound != nullptr && !first) {
-#pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        const int r = i0 + rw + a;
-        const T bound = r < n ? (T)Key<float>::dec(gbound[r]) : T(INFINITY);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (acc[a][q] > bound) acc[a][q] = T(NAN);  // never selected
-      }
-    }
-    // rows with a candidate that beats their current K-th entry (all rows on
-    // a split's first tile, which is sorted whole)
+    // rows that may take a candidate: one at or below both the row's current
+    // K-th distance and the other column ranges' bound for the row (a candidate
+    // farther than some range's K-th distance cannot be among the row's K
+    // nearest; fp32 with several ranges, otherwise no bound). The exact tests
+    // follow for these rows only. A split's first tile is sorted whole.
     unsigned todo = 0;
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-      const T tv = lv[(rw + a) * K + K - 1];
-      const int ti = li[(rw + a) * K + K - 1];
+      const int r = i0 + rw + a;
+      T thr = lv[(rw + a) * K + K - 1];
+      if (gbound != nullptr && r < n) thr = fmin(thr, (T)Key<float>::dec(gbound[r]));
       bool any = first;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) any = any || lexless(acc[a][q], j0 + 4 * lane + q, tv, ti);
-      if (__ballot_sync(0xffffffffu, any) && i0 + rw + a < n) todo |= 1u << a;
+      for (int q = 0; q < 4; ++q) any = any || acc[a][q] <= thr;
+      if (__ballot_sync(0xffffffffu, any) && r < n) todo |= 1u << a;
     }
     // those rows one at a time (a rolled loop keeps the sort and insert code
     // single), reading their distances back from the warp's staging area
@@ -374,6 +365,12 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 1)
         __syncwarp();
         if (gbound != nullptr && lane == 0) publish_bound(gbound + i0 + rw + a, Lv[K - 1]);
         continue;
+      }
+      if (gbound != nullptr) {
+        const T bound = (T)Key<float>::dec(gbound[i0 + rw + a]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (d4[q] > bound) d4[q] = T(NAN);  // never selected
       }
       T tv = Lv[K - 1];
       int ti = Li[K - 1];
