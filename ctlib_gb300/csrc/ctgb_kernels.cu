@@ -493,8 +493,14 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
   }
 }
 
+// Register cap: 96 for the two-step fp32 kernels, where holding a whole line's
+// loads in flight beats the extra warps (2.53 against 2.79 ms for A on the
+// 16-slice fan-ED 512 batch); 72 for the three-step and fp64 ones.
+template <class T, int U>
+constexpr int det_max_regs() { return (sizeof(T) == 4 && U == 2) ? 96 : 72; }
+
 template <class T, int SB, int KIND, int U, bool RES = false>
-__global__ void __maxnreg__(72) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
+__global__ void __maxnreg__((det_max_regs<T, U>())) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
                                                     const T* __restrict__ imy, T* __restrict__ out, int B,
                                                     ResidualOut<T> ro) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
