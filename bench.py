@@ -487,7 +487,8 @@ def run_ours(args):
     achieved_gbs = alg_bytes / (dom_ms / 1e3) / 1e9
     peak = _fp32_peak(dev) if rank == 0 else None
     roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak[0], "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(dom.split()[0]), "peak_source": hbm_peak[1],
+            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(dom.split()[0], args.workload),
+            "peak_source": hbm_peak[1],
             "kernel": dom, "kernel_ms": dom_ms, "algorithmic_bytes": alg_bytes,
             "timing": "CUDA events recorded by the library right around the kernel, mean of the timed steps"}
     roof_fp32 = None
@@ -642,16 +643,20 @@ def _measured(key, fallback):
         return fallback, "fallback"
 
 
-def _ncu_traffic(kernel: str):
+def _ncu_traffic(kernel: str, workload: str):
     """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
-    summary (profiles/dram_traffic.json, written from an ncu capture of the
-    same workload and schedule), or None."""
+    summary (profiles/dram_traffic.json, written from an ncu capture of one
+    workload and its tuned schedule), or None when that summary covers another
+    workload."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(path) as f:
-            entry = json.load(f).get("kernels", {}).get(kernel)
+            summary = json.load(f)
     except (OSError, ValueError):
         return None
+    if summary.get("workload_key") != workload:
+        return None
+    entry = summary.get("kernels", {}).get(kernel)
     return None if entry is None else entry.get("bytes_per_launch")
 
 
