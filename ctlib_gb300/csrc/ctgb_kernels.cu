@@ -220,20 +220,23 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) 
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// CTA b (thread 0) prefetches chunk b, b + gridDim.x, ... of the concatenated list
+// CTA b (thread 0) prefetches chunk b, b + gridDim.x, ... of the concatenated
+// list, visiting only its own chunks (a handful of steps, so the warp holding
+// thread 0 is not held back from its share of the layout work)
 __device__ __forceinline__ void prefetch_tables(const PrefetchList& L) {
   if (threadIdx.x != 0) return;
-  unsigned long long chunk = 0;
+  unsigned long long first = 0;  // global index of table t's first chunk
+  unsigned long long c = blockIdx.x;
   for (int t = 0; t < L.n; ++t) {
     const unsigned long long nb = L.bytes[t];
     const unsigned long long nch = (nb + kPrefetchChunk - 1) / kPrefetchChunk;
-    for (unsigned long long c = 0; c < nch; ++c, ++chunk) {
-      if (chunk % gridDim.x != blockIdx.x) continue;
-      const unsigned long long off = c * kPrefetchChunk;
+    for (; c < first + nch; c += gridDim.x) {
+      const unsigned long long off = (c - first) * kPrefetchChunk;
       unsigned len = (unsigned)((nb - off) < kPrefetchChunk ? (nb - off) : kPrefetchChunk);
       len &= ~15u;  // bulk prefetch sizes are multiples of 16 bytes
       if (len) l2_prefetch_bulk(static_cast<const unsigned char*>(L.ptr[t]) + off, len);
     }
+    first += nch;
   }
 }
 
@@ -261,20 +264,21 @@ __global__ void k_layout_image(const T* __restrict__ img, T* __restrict__ imx, T
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   prefetch_tables(pf);
   const size_t sx = (size_t)round8(W) * SB, sy = (size_t)round8(H) * SB;
-  const size_t n = (size_t)G * NQ * H * W;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % W);
-    const int r = (int)((i / W) % H);
-    const int qd = (int)((i / ((size_t)W * H)) % NQ);
-    const int g = (int)(i / ((size_t)W * H * NQ));
-    T v[QW];
+  const int rows = G * NQ * H;  // (g, qd, r), r fastest; a CTA walks the columns of one row
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int r = row % H, qd = (row / H) % NQ, g = row / (H * NQ);
+    T* ox = imx + ((size_t)g * H + r) * sx + qd * 8 * QW;
+    T* oy = imy + (size_t)g * W * sy + blk_off<SB>(H - 1 - r) + qd * 8 * QW;
+    for (int c = threadIdx.x; c < W; c += blockDim.x) {
+      T v[QW];
 #pragma unroll
-    for (int j = 0; j < QW; ++j) {
-      const int b = g * SB + qd * QW + j;
-      v[j] = b < B ? img[((size_t)b * H + r) * W + c] : T(0);
+      for (int j = 0; j < QW; ++j) {
+        const int b = g * SB + qd * QW + j;
+        v[j] = b < B ? img[((size_t)b * H + r) * W + c] : T(0);
+      }
+      store_q<T, QW>(ox + blk_off<SB>(c), v);
+      store_q<T, QW>(oy + (size_t)c * sy, v);
     }
-    store_q<T, QW>(imx + ((size_t)g * H + r) * sx + blk_off<SB>(c) + qd * 8 * QW, v);
-    store_q<T, QW>(imy + ((size_t)g * W + c) * sy + blk_off<SB>(H - 1 - r) + qd * 8 * QW, v);
   }
 }
 
@@ -286,26 +290,27 @@ __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const 
                               const T* __restrict__ f, int B, int V, int D, int Dp, int G, PrefetchList pf) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   prefetch_tables(pf);
-  const size_t n = (size_t)G * V * NQ * Dp;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int d = (int)(i % Dp);
-    const int qd = (int)((i / Dp) % NQ);
-    const int v = (int)((i / ((size_t)Dp * NQ)) % V);
-    const int g = (int)(i / ((size_t)Dp * NQ * V));
-    T val[QW];
-    if (d < D) {
-      const int de = (flags[v] & 2) ? D - 1 - d : d;
-      const T fac = f ? f[(size_t)v * D + d] : T(1);
+  const int rows = G * V * NQ;  // (g, v, qd), qd fastest; a CTA walks the cells of one row
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int qd = row % NQ, v = (row / NQ) % V, g = row / (NQ * V);
+    const bool flip = flags[v] & 2;
+    T* out = q + (size_t)row * Dp * QW;
+    for (int d = threadIdx.x; d < Dp; d += blockDim.x) {
+      T val[QW];
+      if (d < D) {
+        const int de = flip ? D - 1 - d : d;
+        const T fac = f ? f[(size_t)v * D + d] : T(1);
 #pragma unroll
-      for (int j = 0; j < QW; ++j) {
-        const int b = g * SB + qd * QW + j;
-        val[j] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
+        for (int j = 0; j < QW; ++j) {
+          const int b = g * SB + qd * QW + j;
+          val[j] = b < B ? y[((size_t)b * V + v) * D + de] * fac : T(0);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < QW; ++j) val[j] = T(0);
       }
-    } else {
-#pragma unroll
-      for (int j = 0; j < QW; ++j) val[j] = T(0);
+      store_q<T, QW>(out + (size_t)d * QW, val);
     }
-    store_q<T, QW>(q + i * QW, val);
   }
 }
 
@@ -1347,9 +1352,8 @@ static int launch_det(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   T* imx = static_cast<T*>(ws);
   T* imy = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + al((size_t)G * g.H * round8(g.W) * SB * sizeof(T)));
-  const size_t n = (size_t)G * g.H * g.W;
   const int tb = 256;
-  const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
+  const int nb = (int)std::min<size_t>((size_t)G * Planes<SB>::NQ * g.H, 152 * 16);
   PrefetchList pf{};
   const size_t VL = (size_t)g.V * g.L, VD = (size_t)g.V * g.D;
   pf.ptr[0] = P.lg; pf.bytes[0] = VL * 4 * sizeof(T);
@@ -1396,9 +1400,8 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
     }
     k_ramp_filter<T, SB><<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
   } else if (!planes_ready) {
-    const size_t n = (size_t)G * g.V * P.Dp;
     const int tb = 256;
-    const int nb = (int)std::min<size_t>((n + tb - 1) / tb, 152 * 16);
+    const int nb = (int)std::min<size_t>((size_t)G * g.V * Planes<SB>::NQ, 152 * 16);
     PrefetchList pf{};
     const size_t VL = (size_t)g.V * g.L;
     pf.ptr[0] = P.lp; pf.bytes[0] = VL * 4 * sizeof(T);
