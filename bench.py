@@ -6,6 +6,7 @@ operator for all 16 slices). A ray-update is one (slice, view, detector bin,
 image line); one step is 2 * 16 * 1152 * 736 * 512 = 1.39e10 ray-updates.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--impl ours|reference] --operators   # each operator alone
 
 Prints one JSON line (rank 0). Timing: CUDA events on the launching stream around
 each step, L2 flushed (256 MB write) before every timed step, max over ranks.
@@ -220,6 +221,85 @@ def run_laplacian_only(args):
         return statistics.mean(ts)
 
     print(json.dumps({"only_laplacian": True, **_laplacian_timing(lambda x, k: ctlib.laplacian(x, k), timed, dev)}),
+          flush=True)
+    return 0
+
+
+OPERATORS = ("projection", "projection_t", "backprojection", "backprojection_t", "fbp", "backprojection_sv",
+             "backprojection_sv_1")
+
+
+def run_operators(args):
+    """One JSON line: each operator of the public API alone on the workload's
+    batch, mean ms over K calls after W warm-up calls, L2 flushed before every
+    timed call, CUDA events on the launching stream. backprojection_sv (equal-
+    distance fans only) writes one image per view: it runs on the whole batch
+    when that output fits in 24 GB, and as backprojection_sv_1 on one slice.
+    --impl reference times the reference's own CUDA kernels through
+    oracle/ref_cuda.py instead (fbp: its weighting, taps, torch conv2d and
+    backprojection kernel)."""
+    import torch
+    from ctlib_gb300.workloads import WORKLOADS, phantoms
+    w = WORKLOADS[args.workload]()
+    if not w.uniform:
+        raise SystemExit("--operators needs a uniform workload")
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    img = torch.from_numpy(np.stack(phantoms(w))[:, None]).contiguous().to(dev)
+    opts = torch.tensor(w.slices[0].options, dtype=torch.float32, device=dev)
+    if args.impl == "reference":
+        from oracle import ref_cuda
+        if not ref_cuda.available():
+            print(json.dumps({"impl": "reference", "operators": None,
+                              "unavailable": "reference cubins not built"}), flush=True)
+            return 0
+        ref = ref_cuda.get()
+        sino = ref.run(0, img, opts)
+        calls = {"projection": lambda: ref.run(0, img, opts), "projection_t": lambda: ref.run(1, sino, opts),
+                 "backprojection": lambda: ref.run(2, sino, opts), "backprojection_t": lambda: ref.run(3, img, opts),
+                 "fbp": lambda: ref.fbp(sino, opts), "backprojection_sv": lambda: ref.run(5, sino, opts),
+                 "backprojection_sv_1": lambda: ref.run(5, sino[:1], opts)}
+    else:
+        import ctlib_gb300 as ctlib
+        from ctlib_gb300 import _native as N
+        sino = ctlib.projection(img, opts)
+        if not args.no_tune:
+            from ctlib_gb300 import tune
+            plan = ctlib.get_plan(opts, torch.float32, dev)
+            for op in (N.OP_PROJECTION, N.OP_PROJECTION_T, N.OP_BACKPROJECTION, N.OP_BACKPROJECTION_T, N.OP_FBP):
+                tune.tune(plan, op, img.shape[0])
+        calls = {"projection": lambda: ctlib.projection(img, opts),
+                 "projection_t": lambda: ctlib.projection_t(sino, opts),
+                 "backprojection": lambda: ctlib.backprojection(sino, opts),
+                 "backprojection_t": lambda: ctlib.backprojection_t(img, opts), "fbp": lambda: ctlib.fbp(sino, opts),
+                 "backprojection_sv": lambda: ctlib.backprojection_sv(sino, opts),
+                 "backprojection_sv_1": lambda: ctlib.backprojection_sv(sino[:1], opts)}
+    res = {}
+    # backprojection_sv exists for equal-distance fans only (src/fan_ed_kernel.cu:946-1161)
+    names = list(OPERATORS if w.slices[0].scan_type == 0 else OPERATORS[:-2])
+    if "backprojection_sv" in names and img.numel() * sino.shape[-2] * 4 > 24e9:  # B x V x H x W floats
+        names.remove("backprojection_sv")
+    for name in names:
+        fn = calls[name]
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        slices = 1 if name == "backprojection_sv_1" else img.shape[0]
+        ms = statistics.mean(ts)
+        res[name] = {"ms": ms, "slices": slices,
+                     "ray_updates_per_s": w.ray_updates() * slices / img.shape[0] / (ms / 1e3)}
+    print(json.dumps({"impl": args.impl, "workload": args.workload, "batch": img.shape[0], "operators": res,
+                      "timing": "mean of K calls, L2 flushed before each, CUDA events on the launching stream"}),
           flush=True)
     return 0
 
@@ -672,11 +752,15 @@ def main():
                     help="time only the batched projection + projection_t step (for profiler runs)")
     ap.add_argument("--only-laplacian", action="store_true",
                     help="time only the laplacian case (16384 points, dimension 64, k = 16; for profiler runs)")
+    ap.add_argument("--operators", action="store_true",
+                    help="time each operator of the API alone on the workload (both arms)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
     if args.only_laplacian:
         return run_laplacian_only(args)
+    if args.operators:
+        return run_operators(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload.startswith("ragged"):
