@@ -267,8 +267,13 @@ def run_operators(args):
         if not args.no_tune:
             from ctlib_gb300 import tune
             plan = ctlib.get_plan(opts, torch.float32, dev)
-            for op in (N.OP_PROJECTION, N.OP_PROJECTION_T, N.OP_BACKPROJECTION, N.OP_BACKPROJECTION_T, N.OP_FBP):
+            ops = [N.OP_PROJECTION, N.OP_PROJECTION_T, N.OP_BACKPROJECTION, N.OP_BACKPROJECTION_T, N.OP_FBP]
+            if w.slices[0].scan_type == 0:
+                ops.append(N.OP_BACKPROJECTION_SV)
+            for op in ops:
                 tune.tune(plan, op, img.shape[0])
+                if op == N.OP_BACKPROJECTION_SV:
+                    tune.tune(plan, op, 1)
         calls = {"projection": lambda: ctlib.projection(img, opts),
                  "projection_t": lambda: ctlib.projection_t(sino, opts),
                  "backprojection": lambda: ctlib.backprojection(sino, opts),

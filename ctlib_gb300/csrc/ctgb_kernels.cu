@@ -811,11 +811,12 @@ struct PixSlot {
 // SV: single-view backprojection (src/fan_ed_kernel.cu:946-1161): each view's
 // sum goes to its own image, img[slice][view][row][col], with no sum over views.
 //
-// nsplit (1 or 2): blockIdx.z = slice group * nsplit + part, and part p sums
-// views [V*p/nsplit, V*(p+1)/nsplit). With two parts each adds its scaled sum
-// into the zeroed output with one atomic add; 0 + a + b is the same in either
-// order, so the result is deterministic. Shorter CTAs fill the last wave of a
-// grid that is only a few waves deep.
+// nsplit: blockIdx.z = slice group * nsplit + part, and part p takes views
+// [V*p/nsplit, V*(p+1)/nsplit). Summing operators use 1 or 2 parts: with two,
+// each adds its scaled sum into the zeroed output with one atomic add; 0 + a + b
+// is the same in either order, so the result is deterministic. SV writes every
+// view's image directly, so it takes any number of parts. Shorter CTAs fill the
+// last wave of a grid that is only a few waves deep.
 template <class T, int SB, int KIND, int U, bool SV = false>
 __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div,
@@ -1418,8 +1419,11 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   auto launch = [&](auto kern, T mul, T div) -> int {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
-    const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? 1 : view_split(g.V);
-    if (nsplit > 1) {
+    // single-view backprojection writes each view's image on its own, so its views
+    // split over any number of CTAs with no adds: 8 parts shorten the CTAs of a
+    // grid that is only ~2 waves deep (7.62 to 6.85 ms for 16 x 512^2, 1152 views)
+    const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? std::min(8, g.V) : view_split(g.V);
+    if (nsplit > 1 && op != CTGB_OP_BACKPROJECTION_SV) {
       e = cudaMemsetAsync(y, 0, (size_t)batch * g.H * g.W * sizeof(T), st);
       if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather clear: ") + cudaGetErrorString(e));
     }

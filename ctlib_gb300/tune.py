@@ -100,6 +100,9 @@ def _inputs(plan, op: int, batch: int):
     sino = (batch, 1, plan.views, plan.dets)
     if op in (N.OP_PROJECTION, N.OP_BACKPROJECTION_T):
         return torch.rand(img, dtype=plan.dtype, device=dev), torch.empty(sino, dtype=plan.dtype, device=dev)
+    if op == N.OP_BACKPROJECTION_SV:  # one image per view
+        views = (batch, plan.views, plan.height, plan.width)
+        return torch.randn(sino, dtype=plan.dtype, device=dev), torch.empty(views, dtype=plan.dtype, device=dev)
     return torch.randn(sino, dtype=plan.dtype, device=dev), torch.empty(img, dtype=plan.dtype, device=dev)
 
 
