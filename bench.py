@@ -243,6 +243,8 @@ def run_operators(args):
     w = WORKLOADS[args.workload]()
     if not w.uniform:
         raise SystemExit("--operators needs a uniform workload")
+    if args.batch:
+        w.slices = w.slices[:1] * args.batch
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -759,6 +761,7 @@ def main():
                     help="time only the laplacian case (16384 points, dimension 64, k = 16; for profiler runs)")
     ap.add_argument("--operators", action="store_true",
                     help="time each operator of the API alone on the workload (both arms)")
+    ap.add_argument("--batch", type=int, default=0, help="with --operators: slices per call (default: the workload's)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1

@@ -317,16 +317,21 @@ __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const 
 // ----------------------------------------------------------------------------
 // backprojector pixel weights
 // ----------------------------------------------------------------------------
+// The sums of two products are written as one explicit FMA over one rounded
+// product: left to the compiler, which product it fuses can differ between
+// inlined copies, and every copy (staged or global view, one or more pixels per
+// thread, any schedule) must give the same weight bit for bit.
 // U^2 weight (src/fan_ed_kernel.cu:18-21)
 template <class T>
 __device__ __forceinline__ T cweight_ed(T sx, T sy, T x, T y, T r) {
-  const T d = (sx * x + sy * y) / r;
+  const T d = fma(sx, x, mul_rn(sy, y)) / r;
   return r * r / ((r - d) * (r - d));
 }
 // squared source distance (src/fan_ea_kernel.cu:18-20), used as a divisor
 template <class T>
 __device__ __forceinline__ T dist2_ea(T sx, T sy, T x, T y) {
-  return (sx - x) * (sx - x) + (sy - y) * (sy - y);
+  const T ex = sx - x, ey = sy - y;
+  return fma(ex, ex, mul_rn(ey, ey));
 }
 
 // ----------------------------------------------------------------------------
@@ -785,23 +790,34 @@ __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int 
 // ragged path sums the same halves and matches too.
 __host__ __device__ __forceinline__ int view_split(int views) { return views >= 64 ? 2 : 1; }
 
-// Staged image gather. A CTA is a 32 x R pixel tile (R consumer warps, lane =
-// column, warp = row) plus one producer warp. For each view the producer finds
+// Staged image gather. A CTA is a 32 x (R * PX) pixel tile plus one producer
+// warp: R consumer warps, lane = column, and warp w owns rows w, w + R, ...,
+// w + (PX - 1) R, so that the per-view costs of a warp (barrier, slot header,
+// loop) are shared by PX pixels where one slice leaves them unshared (PX > 1
+// for one slice per thread). For each view the producer finds
 // the tile's cell footprint from its four corner pixel edges (exact extremes:
 // along a line the edges grow with k, and across lines each edge moves
 // monotonically because the source lies outside the image), and when it fits
-// kWin cells it copies the cell records, the q planes of those cells and the
-// tile's line maps into a ring of kSlots shared-memory slots with TMA bulk
+// the slot's window of cells it copies the cell records, the q planes of those
+// cells and the tile's line maps into a ring of kSlots shared-memory slots with TMA bulk
 // copies. Consumers then read only shared memory; a view whose footprint does
 // not fit is read from the global tables instead (same arithmetic, same
 // result). The window carries a margin of two cells on each side, so every cell
 // a pixel can reach (including the seed correction and the step back when the
 // offset is negative) lies inside it.
-constexpr int kWin = 64;   // cells per staged view window (multiple of 4)
 constexpr int kSlots = 7;  // views in flight per CTA
+
+// pixel rows per consumer thread of the staged image gather: 2 for one slice
+// per thread, whose per-view costs are otherwise borne by one pixel alone
+// (2.10 to 1.65 ms for A^T of one 512^2 slice, 1152 views; 4 rows: 1.90 ms)
+template <int SB>
+constexpr int kPixRows = SB == 1 ? 2 : 1;
 
 template <class T, int SB>
 struct PixSlot {
+  // cells per staged view window (multiple of 4): one- and two-slice slots are
+  // small, so they take the wider footprints of the taller pixel-blocked tiles
+  static constexpr int kWin = SB <= 2 ? 128 : 64;
   static constexpr int kQBytes = SB * kWin * (int)sizeof(T);    // NQ planes x kWin cells x QW
   static constexpr int kRecBytes = kWin * 4 * (int)sizeof(T);   // kWin records
   static constexpr int kLpBytes = 32 * 4 * (int)sizeof(T);      // up to 32 line maps
@@ -817,12 +833,13 @@ struct PixSlot {
 // is the same in either order, so the result is deterministic. SV writes every
 // view's image directly, so it takes any number of parts. Shorter CTAs fill the
 // last wave of a grid that is only a few waves deep.
-template <class T, int SB, int KIND, int U, bool SV = false>
+template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1>
 __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div,
                                                        int nsplit) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
+  constexpr int kWin = S::kWin;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
   __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
   // slot header, two 16-byte words: (window start or -1, flags, first line,
@@ -834,9 +851,9 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   const int R = (int)(blockDim.x >> 5) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int CT = 32 * R;                     // consumer threads
-  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][SB][CT]: running sum, compensation
-  unsigned char* slots = pix_smem + (size_t)2 * SB * CT * sizeof(T);
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R;
+  T* acc = reinterpret_cast<T*>(pix_smem);  // [2][PX * SB][CT]: running sum, compensation
+  unsigned char* slots = pix_smem + (size_t)2 * PX * SB * CT * sizeof(T);
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R * PX;
   const int part = blockIdx.z % nsplit, g = blockIdx.z / nsplit;
   const int V = P.V, D = P.D, Dp = P.Dp;
   const int vbeg = (int)((long long)V * part / nsplit), vend = (int)((long long)V * (part + 1) / nsplit);
@@ -853,7 +870,7 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   __syncthreads();
 
   if (warp == R) {  // producer
-    const int c1 = min(c0 + 32, P.W) - 1, r1 = min(r0 + R, P.H) - 1;
+    const int c1 = min(c0 + 32, P.W) - 1, r1 = min(r0 + R * PX, P.H) - 1;
     // Per-view inputs of the window search, loaded for view vb + lane one batch
     // of 32 views ahead so that their latency overlaps the copies of the batch
     // before; the search itself (seed, then the bracketing boundaries) costs
@@ -968,15 +985,27 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
     return;
   }
 
-  // consumers
-  const int c = c0 + lane, r = r0 + warp;
-  const bool active = c < P.W && r < P.H;
-  const T pcx = active ? P.colc[c] : T(0);
-  const T pcy = active ? P.rowc[r] : T(0);
-  kahan_init_smem<T, SB>(acc, CT);
-  T blk[SB];
+  // consumers: pixels (r[p], c), p < PX; acc holds [PX][2][SB][CT]
+  const int c = c0 + lane;
+  int rp[PX];
+  bool act[PX];
+  T pcy[PX];
+  bool any = false;
 #pragma unroll
-  for (int s = 0; s < SB; ++s) blk[s] = T(0);
+  for (int p = 0; p < PX; ++p) {
+    rp[p] = r0 + warp + p * R;
+    act[p] = c < P.W && rp[p] < P.H;
+    pcy[p] = act[p] ? P.rowc[rp[p]] : T(0);
+    any = any || act[p];
+  }
+  const T pcx = any ? P.colc[c] : T(0);
+  T blk[PX][SB];
+#pragma unroll
+  for (int p = 0; p < PX; ++p) {
+    kahan_init_smem<T, SB>(acc + (size_t)p * 2 * SB * CT, CT);
+#pragma unroll
+    for (int s = 0; s < SB; ++s) blk[p][s] = T(0);
+  }
   for (int u = 0; u < NV; ++u) {
     const int v = vbeg + u, slot = u % kSlots;
     bool ok = false;
@@ -986,9 +1015,11 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
     }
     if (SV) {
 #pragma unroll
-      for (int s = 0; s < SB; ++s) blk[s] = T(0);
+      for (int p = 0; p < PX; ++p)
+#pragma unroll
+        for (int s = 0; s < SB; ++s) blk[p][s] = T(0);
     }
-    if (active) {
+    if (any) {
       const int4 h0 = ok ? s_hdr[slot][0] : make_int4(-1, 0, 0, 0);
       if (h0.x >= 0) {
         const int4 h1 = s_hdr[slot][1];
@@ -999,40 +1030,56 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         const T* sq = reinterpret_cast<const T*>(sl);
         const T* srec = reinterpret_cast<const T*>(sl + S::kQBytes);
         const T* slp = reinterpret_cast<const T*>(sl + S::kQBytes + S::kRecBytes);
-        const Quad<T> A4 = ldrec<T, true>(slp + ((xb ? r : c) - h0.z) * 4);
         T sx = T(0), sy = T(0);
         if (KIND == kB) { sx = s_src[slot][0]; sy = s_src[slot][1]; }
-        pix_view<T, SB, KIND, U, true>(P, A4, xb ? c : P.H - 1 - r, sd, sx, sy, pcx, pcy, srec, sq, kWin, h0.x,
-                                       h0.x, min(h0.x + kWin, D), blk);
+#pragma unroll
+        for (int p = 0; p < PX; ++p) {
+          if (PX > 1 && !act[p]) continue;
+          const Quad<T> A4 = ldrec<T, true>(slp + ((xb ? rp[p] : c) - h0.z) * 4);
+          pix_view<T, SB, KIND, U, true>(P, A4, xb ? c : P.H - 1 - rp[p], sd, sx, sy, pcx, pcy[p], srec, sq, kWin,
+                                         h0.x, h0.x, min(h0.x + kWin, D), blk[p]);
+        }
       } else {
-        pix_view_global<T, SB, KIND, U>(P, v, r, c, qg + (size_t)v * NQ * Dp * QW, Dp, pcx, pcy, blk);
+#pragma unroll
+        for (int p = 0; p < PX; ++p) {
+          if (PX > 1 && !act[p]) continue;
+          pix_view_global<T, SB, KIND, U>(P, v, rp[p], c, qg + (size_t)v * NQ * Dp * QW, Dp, pcx, pcy[p], blk[p]);
+        }
       }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&s_empty[slot]);
     if (SV) {
-      if (active) {
+#pragma unroll
+      for (int p = 0; p < PX; ++p) {
+        if (!act[p]) continue;
 #pragma unroll
         for (int s = 0; s < SB; ++s) {
           const int bb = g * SB + s;
-          if (bb < B) img[(((size_t)bb * V + v) * P.H + r) * P.W + c] = blk[s];
+          if (bb < B) img[(((size_t)bb * V + v) * P.H + rp[p]) * P.W + c] = blk[p][s];
         }
       }
     } else if ((u % kFoldEvery) == kFoldEvery - 1) {
-      kahan_fold_smem<T, SB>(acc, blk, CT);
+#pragma unroll
+      for (int p = 0; p < PX; ++p) kahan_fold_smem<T, SB>(acc + (size_t)p * 2 * SB * CT, blk[p], CT);
     }
   }
-  if (SV) return;
-  kahan_fold_smem<T, SB>(acc, blk, CT);
-  if (!active) return;
+  if constexpr (!SV) {
 #pragma unroll
-  for (int s = 0; s < SB; ++s) {
-    const int bb = g * SB + s;
-    if (bb >= B) continue;
-    const T val = acc[(size_t)s * CT + threadIdx.x] * out_mul / out_div;
-    T* dst = img + ((size_t)bb * P.H + r) * P.W + c;
-    if (nsplit == 1) *dst = val;
-    else atomicAdd(dst, val);
+    for (int p = 0; p < PX; ++p) {
+      T* ap = acc + (size_t)p * 2 * SB * CT;
+      kahan_fold_smem<T, SB>(ap, blk[p], CT);
+      if (!act[p]) continue;
+#pragma unroll
+      for (int s = 0; s < SB; ++s) {
+        const int bb = g * SB + s;
+        if (bb >= B) continue;
+        const T val = ap[(size_t)s * CT + threadIdx.x] * out_mul / out_div;
+        T* dst = img + ((size_t)bb * P.H + rp[p]) * P.W + c;
+        if (nsplit == 1) *dst = val;
+        else atomicAdd(dst, val);
+      }
+    }
   }
 }
 
@@ -1412,10 +1459,11 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
     k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr, batch,
                                            g.V, g.D, P.Dp, G, pf);
   }
-  const int wpc = p->warps[sched];  // consumer warps (one pixel row each) + one producer warp
-  dim3 grid((g.W + 31) / 32, (g.H + wpc - 1) / wpc, G);
+  const int wpc = p->warps[sched];  // consumer warps (PX pixel rows each) + one producer warp
+  constexpr int PX = kPixRows<SB>;
+  dim3 grid((g.W + 31) / 32, (g.H + wpc * PX - 1) / (wpc * PX), G);
   const int nt = 32 * (wpc + 1);
-  const size_t smem = (size_t)2 * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
+  const size_t smem = (size_t)2 * PX * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
   auto launch = [&](auto kern, T mul, T div) -> int {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
@@ -1435,13 +1483,16 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
   const bool two = kTwoStep<T, SB> && p->unroll[sched] == 2;
   if (op == CTGB_OP_BACKPROJECTION_SV)
-    return two ? launch(k_pix_gather<T, SB, kB, U2, true>, T(1), T(1))
-               : launch(k_pix_gather<T, SB, kB, 3, true>, T(1), T(1));
+    return two ? launch(k_pix_gather<T, SB, kB, U2, true, PX>, T(1), T(1))
+               : launch(k_pix_gather<T, SB, kB, 3, true, PX>, T(1), T(1));
   if (op == CTGB_OP_PROJECTION_T)
-    return two ? launch(k_pix_gather<T, SB, kAt, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kAt, 3>, T(1), T(1));
+    return two ? launch(k_pix_gather<T, SB, kAt, U2, false, PX>, T(1), T(1))
+               : launch(k_pix_gather<T, SB, kAt, 3, false, PX>, T(1), T(1));
   if (op == CTGB_OP_BACKPROJECTION)
-    return two ? launch(k_pix_gather<T, SB, kB, U2>, T(1), T(1)) : launch(k_pix_gather<T, SB, kB, 3>, T(1), T(1));
-  return two ? launch(k_pix_gather<T, SB, kB, U2>, P.dAng, T(2)) : launch(k_pix_gather<T, SB, kB, 3>, P.dAng, T(2));
+    return two ? launch(k_pix_gather<T, SB, kB, U2, false, PX>, T(1), T(1))
+               : launch(k_pix_gather<T, SB, kB, 3, false, PX>, T(1), T(1));
+  return two ? launch(k_pix_gather<T, SB, kB, U2, false, PX>, P.dAng, T(2))
+             : launch(k_pix_gather<T, SB, kB, 3, false, PX>, P.dAng, T(2));
 }
 
 template <class T, int SB>
