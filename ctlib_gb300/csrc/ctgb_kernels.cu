@@ -793,8 +793,8 @@ __host__ __device__ __forceinline__ int view_split(int views) { return views >= 
 // Staged image gather. A CTA is a 32 x (R * PX) pixel tile plus one producer
 // warp: R consumer warps, lane = column, and warp w owns rows w, w + R, ...,
 // w + (PX - 1) R, so that the per-view costs of a warp (barrier, slot header,
-// loop) are shared by PX pixels where one slice leaves them unshared (PX > 1
-// for one slice per thread). For each view the producer finds
+// loop) are shared by PX pixels where few slices leave them poorly shared
+// (PX = 2 up to 8 slices per thread). For each view the producer finds
 // the tile's cell footprint from its four corner pixel edges (exact extremes:
 // along a line the edges grow with k, and across lines each edge moves
 // monotonically because the source lies outside the image), and when it fits
@@ -807,11 +807,12 @@ __host__ __device__ __forceinline__ int view_split(int views) { return views >= 
 // offset is negative) lies inside it.
 constexpr int kSlots = 7;  // views in flight per CTA
 
-// pixel rows per consumer thread of the staged image gather: 2 for one slice
-// per thread, whose per-view costs are otherwise borne by one pixel alone
-// (2.10 to 1.65 ms for A^T of one 512^2 slice, 1152 views; 4 rows: 1.90 ms)
+// pixel rows per consumer thread of the staged image gather: 2 up to 8 slices
+// per thread, where the per-view costs are shared by few slices (A^T of one
+// 512^2 slice, 1152 views: 2.10 to 1.65 ms, 4 rows 1.90 ms; of 8 slices: 2.25
+// to 1.95 ms); 1 for 16 slices, whose 32 sums would not fit 72 registers
 template <int SB>
-constexpr int kPixRows = SB == 1 ? 2 : 1;
+constexpr int kPixRows = SB <= 8 ? 2 : 1;
 
 template <class T, int SB>
 struct PixSlot {
