@@ -9,6 +9,12 @@ Every stage of an operator is a single persistent launch over all slices
 per-slice pointers are kernel parameters, so a run can be captured in a CUDA
 graph: ``rb.graphed(op, inputs)`` returns a replayable callable over static
 input/output buffers.
+
+``rb.graphed(op, inputs, branches=k)`` (the default, k = 4) instead captures
+each slice's own per-slice launches (the staged image gather included) on k
+parallel branches of the graph, slices assigned longest first to the least
+loaded branch: no launch or plan overhead per call, and small slices overlap
+one another. ``branches=0`` captures the persistent launches.
 """
 
 from __future__ import annotations
@@ -18,7 +24,8 @@ import ctypes
 import torch
 
 from . import _native as N
-from .ops import get_plan
+from . import tune
+from .ops import _FN, get_plan
 
 _OPS = {"projection": N.OP_PROJECTION, "projection_t": N.OP_PROJECTION_T, "backprojection": N.OP_BACKPROJECTION,
         "backprojection_t": N.OP_BACKPROJECTION_T, "fbp": N.OP_FBP}
@@ -94,14 +101,20 @@ class RaggedBatch:
     def fbp(self, sinos):
         return self.run(N.OP_FBP, sinos)
 
-    def graphed(self, ops, inputs):
+    def graphed(self, ops, inputs, branches: int = 4):
         """Capture `ops` (one op name or a chain such as ("projection", "fbp"),
         each op consuming the previous one's outputs) into a CUDA graph over
         static copies of `inputs`. Returns (replay, static_inputs, outputs):
-        copy new data into static_inputs, call replay(), read outputs."""
+        copy new data into static_inputs, call replay(), read outputs.
+        branches = k > 0 (default 4): the slices' own launches on k parallel
+        graph branches; branches = 0: the persistent ragged launches."""
         if isinstance(ops, str):
             ops = (ops,)
+        if branches < 0:
+            raise ValueError("branches must be >= 0")
         static_in = [x.clone() for x in inputs]
+        if branches:
+            return self._graphed_branches(ops, static_in, branches)
         bufs, cur = [], static_in
         for name in ops:
             op = _OPS[name]
@@ -120,4 +133,61 @@ class RaggedBatch:
         with torch.cuda.graph(graph):
             for op, i, o, w in bufs:
                 self.run(op, i, o, w)
-        return graph.replay, static_in, cur
+        return _replayer(graph, bufs), static_in, cur
+
+    def _graphed_branches(self, ops, static_in, branches):
+        chains, work = [], []
+        for i, plan in enumerate(self.plans):
+            cur, chain = static_in[i], []
+            for name in ops:
+                op = _OPS[name]
+                tune.apply_cached(plan, op, 1)  # the schedule a per-slice call would use
+                out_shapes, _ = self._shapes(op)
+                out = torch.empty(out_shapes[i], dtype=torch.float32, device=self.device)
+                nbytes = plan.workspace_bytes(op, 1)
+                ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+                chain.append((plan, op, cur, out, ws, nbytes))
+                cur = out
+            chains.append(chain)
+            work.append(plan.views * plan.dets * max(plan.height, plan.width))
+        # longest slices first, each to the least loaded branch
+        load, lanes = [0] * branches, [[] for _ in range(branches)]
+        for i in sorted(range(self.n), key=lambda j: -work[j]):
+            b = min(range(branches), key=lambda k: load[k])
+            load[b] += work[i]
+            lanes[b].append(i)
+        streams = [torch.cuda.Stream(self.device) for _ in range(branches)]
+
+        def issue():
+            main = torch.cuda.current_stream(self.device)
+            for st, lane in zip(streams, lanes):
+                st.wait_stream(main)
+                for i in lane:
+                    for plan, op, x, y, ws, nbytes in chains[i]:
+                        rc = _FN[op](plan.handle, x.data_ptr(), y.data_ptr(), 1, ws.data_ptr(), nbytes,
+                                     st.cuda_stream)
+                        N.check(rc, "ragged branch")
+            for st in streams:
+                main.wait_stream(st)
+
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            issue()  # warm-up outside capture
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            issue()
+        return _replayer(graph, (chains, streams)), static_in, [c[-1][3] for c in chains]
+
+
+def _replayer(graph, buffers):
+    """graph.replay, holding the tensors the graph reads and writes (its
+    intermediate outputs and workspaces): the graph does not own that memory,
+    and once freed the caching allocator would hand it to other tensors."""
+
+    def replay():
+        graph.replay()
+
+    replay.graph, replay.buffers = graph, buffers
+    return replay

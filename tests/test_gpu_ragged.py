@@ -49,15 +49,22 @@ def test_ragged_matches_per_slice_calls(env, op):
         assert torch.equal(y, want), (op, o, float((y - want).abs().max()))
 
 
-def test_ragged_graph_replay(env):
+@pytest.mark.parametrize("branches", [0, 1, 3])
+def test_ragged_graph_replay(env, branches):
     ct, batched = env
     opts = _slices()
     rb = batched.RaggedBatch(opts)
     from ctlib_gb300.workloads import ellipse_phantom
     imgs = [torch.from_numpy(ellipse_phantom(int(o[3]), int(o[2]), o[4], 40 + i)[None, None]).cuda()
             for i, o in enumerate(opts)]
-    replay, static_in, outs = rb.graphed(("projection", "fbp"), imgs)
+    replay, static_in, outs = rb.graphed(("projection", "fbp"), imgs, branches=branches)
+    # the graph's intermediate buffers and workspaces must stay owned by the
+    # replay callable: fresh allocations written between replays must not land
+    # on them
+    junk = [torch.empty(1 << 20, device="cuda") for _ in range(64)]
     for trial in range(2):
+        for t in junk:
+            t.fill_(7.0 + trial)
         for s, x in zip(static_in, imgs):
             s.copy_(x * (1.0 + trial))
         replay()
