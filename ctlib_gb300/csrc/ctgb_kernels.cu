@@ -810,7 +810,8 @@ constexpr int kSlots = 7;  // views in flight per CTA
 // pixel rows per consumer thread of the staged image gather: 2 up to 8 slices
 // per thread, where the per-view costs are shared by few slices (A^T of one
 // 512^2 slice, 1152 views: 2.10 to 1.65 ms, 4 rows 1.90 ms; of 8 slices: 2.25
-// to 1.95 ms); 1 for 16 slices, whose 32 sums would not fit 72 registers
+// to 1.95 ms); 1 for 16 slices, whose 32 sums do not fit 72 registers (2 rows
+// spill: 3.14 against 2.62 ms)
 template <int SB>
 constexpr int kPixRows = SB <= 8 ? 2 : 1;
 
