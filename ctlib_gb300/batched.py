@@ -150,12 +150,7 @@ class RaggedBatch:
                 cur = out
             chains.append(chain)
             work.append(plan.views * plan.dets * max(plan.height, plan.width))
-        # longest slices first, each to the least loaded branch
-        load, lanes = [0] * branches, [[] for _ in range(branches)]
-        for i in sorted(range(self.n), key=lambda j: -work[j]):
-            b = min(range(branches), key=lambda k: load[k])
-            load[b] += work[i]
-            lanes[b].append(i)
+        lanes = assign_branches(work, branches)
         streams = [torch.cuda.Stream(self.device) for _ in range(branches)]
 
         def issue():
@@ -191,3 +186,17 @@ def _replayer(graph, buffers):
 
     replay.graph, replay.buffers = graph, buffers
     return replay
+
+
+def assign_branches(work, branches: int):
+    """Slices (by index) for each of `branches` graph branches: longest slice
+    first, each to the branch with the least work so far (ties to the lower
+    branch), so that the branches end close together."""
+    if branches < 1:
+        raise ValueError("branches must be >= 1")
+    load, lanes = [0] * branches, [[] for _ in range(branches)]
+    for i in sorted(range(len(work)), key=lambda j: -work[j]):
+        b = min(range(branches), key=lambda k: load[k])
+        load[b] += work[i]
+        lanes[b].append(i)
+    return lanes
