@@ -249,8 +249,9 @@ def run_operators(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    img = torch.from_numpy(np.stack(phantoms(w))[:, None]).contiguous().to(dev)
-    opts = torch.tensor(w.slices[0].options, dtype=torch.float32, device=dev)
+    dt = torch.float64 if args.dtype == "f64" else torch.float32
+    img = torch.from_numpy(np.stack(phantoms(w))[:, None]).to(dt).contiguous().to(dev)
+    opts = torch.tensor(w.slices[0].options, dtype=dt, device=dev)
     if args.impl == "reference":
         from oracle import ref_cuda
         if not ref_cuda.available():
@@ -269,7 +270,7 @@ def run_operators(args):
         sino = ctlib.projection(img, opts)
         if not args.no_tune:
             from ctlib_gb300 import tune
-            plan = ctlib.get_plan(opts, torch.float32, dev)
+            plan = ctlib.get_plan(opts, dt, dev)
             ops = [N.OP_PROJECTION, N.OP_PROJECTION_T, N.OP_BACKPROJECTION, N.OP_BACKPROJECTION_T, N.OP_FBP]
             if w.slices[0].scan_type == 0:
                 ops.append(N.OP_BACKPROJECTION_SV)
@@ -286,7 +287,7 @@ def run_operators(args):
     res = {}
     # backprojection_sv exists for equal-distance fans only (src/fan_ed_kernel.cu:946-1161)
     names = list(OPERATORS if w.slices[0].scan_type == 0 else OPERATORS[:-2])
-    if "backprojection_sv" in names and img.numel() * sino.shape[-2] * 4 > 24e9:  # B x V x H x W floats
+    if "backprojection_sv" in names and img.numel() * sino.shape[-2] * img.element_size() > 24e9:  # B x V x H x W
         names.remove("backprojection_sv")
     for name in names:
         fn = calls[name]
@@ -306,7 +307,8 @@ def run_operators(args):
         ms = statistics.mean(ts)
         res[name] = {"ms": ms, "slices": slices,
                      "ray_updates_per_s": w.ray_updates() * slices / img.shape[0] / (ms / 1e3)}
-    print(json.dumps({"impl": args.impl, "workload": args.workload, "batch": img.shape[0], "operators": res,
+    print(json.dumps({"impl": args.impl, "workload": args.workload, "batch": img.shape[0], "dtype": args.dtype,
+                      "operators": res,
                       "timing": "mean of K calls, L2 flushed before each, CUDA events on the launching stream"}),
           flush=True)
     return 0
@@ -772,6 +774,7 @@ def main():
     ap.add_argument("--operators", action="store_true",
                     help="time each operator of the API alone on the workload (both arms)")
     ap.add_argument("--batch", type=int, default=0, help="with --operators: slices per call (default: the workload's)")
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="with --operators: element type")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
