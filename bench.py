@@ -576,9 +576,13 @@ def run_ours(args):
     hbm_peak = _measured("hbm_gbs", 6790.7)
     achieved_gbs = alg_bytes / (dom_ms / 1e3) / 1e9
     peak = _fp32_peak(dev) if rank == 0 else None
+    traffic = _ncu_traffic(dom.split()[0], args.workload)
     roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak[0], "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak[0], "traffic": _ncu_traffic(dom.split()[0], args.workload),
-            "peak_source": hbm_peak[1],
+            "frac": achieved_gbs / hbm_peak[0], "traffic": traffic,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm_peak[1] == "measured" else "fallback 6790.7 GB/s",
+            "traffic_source": ("committed ncu summary profiles/dram_traffic.json (dram__bytes_read.sum + "
+                               "dram__bytes_write.sum of one capture of this workload), not measured in this run"
+                               if traffic is not None else "no ncu capture of this workload"),
             "kernel": dom, "kernel_ms": dom_ms, "algorithmic_bytes": alg_bytes,
             "timing": "CUDA events recorded by the library right around the kernel, mean of the timed steps"}
     roof_fp32 = None
@@ -589,6 +593,8 @@ def run_ours(args):
         ach = ru_dom / (dom_ms / 1e3)
         roof_fp32 = {"achieved": ach, "peak": model_peak, "unit": "ray-updates/s", "frac": ach / model_peak,
                      "model": "8 FP32 lane-ops per ray-update at measured FFMA lane-op rate",
+                     "peak_source": "builder-measured: FFMA lane-op rate of this GPU timed in this run by "
+                                    "ctlib_gb300/csrc/peak_fp32.cu (MEASURED_PEAKS.json has no FP32 figure)",
                      "measured_fp32": peak}
 
     if rank == 0:

@@ -133,7 +133,10 @@ class RaggedBatch:
         with torch.cuda.graph(graph):
             for op, i, o, w in bufs:
                 self.run(op, i, o, w)
-        return _replayer(graph, bufs), static_in, cur
+        # the captured kernels read this batch's device tables (task lists, plan
+        # copies, offsets), which ctgb_ragged_destroy frees: the replay holds
+        # the batch itself, not only the buffers
+        return _replayer(graph, (self, bufs)), static_in, cur
 
     def _graphed_branches(self, ops, static_in, branches):
         chains, work = [], []
@@ -177,9 +180,11 @@ class RaggedBatch:
 
 
 def _replayer(graph, buffers):
-    """graph.replay, holding the tensors the graph reads and writes (its
-    intermediate outputs and workspaces): the graph does not own that memory,
-    and once freed the caching allocator would hand it to other tensors."""
+    """graph.replay, holding what the graph reads and writes: its intermediate
+    outputs and workspaces, and the plans or ragged batch whose device tables
+    its kernels read. The graph owns none of that memory; once freed, the
+    caching allocator would hand the tensors to others and a destroyed plan or
+    batch would leave the kernels reading released device memory."""
 
     def replay():
         graph.replay()

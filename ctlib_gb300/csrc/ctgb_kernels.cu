@@ -26,6 +26,7 @@
 // src/fan_ea_kernel.cu:23-921, src/para_kernel.cu:8-683 (weights, flip and
 // branch rules, Q3 factor of equal-angle B^T at src/fan_ea_kernel.cu:590-607).
 
+#include <cuda.h>  // driver types only (CUcontext, CUresult); no libcuda link
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1723,26 +1724,56 @@ __global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<float>* __restri
 // memory instead of a caller-provided buffer. Its size is fixed: every GPU on
 // which this library's kernels are loaded reserves these bytes until process
 // exit. Host code only knows the array through cudaGetSymbolAddress (the name
-// itself is a host-side stand-in, not a device address); the device address is
-// looked up once per device, with that device current, and cached.
+// itself is a host-side stand-in, not a device address). The device address is
+// looked up with the device current, once per device and CUDA context: the
+// cache is keyed on the context's process-unique ID (cuCtxGetId), so a context
+// torn down and created again (cudaDeviceReset) gets a fresh lookup instead of
+// a dead address.
 constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;  // 64 MiB
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_dev_ptr[256] = {};
+struct NoAllocEntry {
+  unsigned long long ctx_id;  // 0: not looked up yet (context IDs start at 1)
+  void* ptr;
+};
+static NoAllocEntry g_noalloc_dev[256] = {};
+
+// ID of the calling thread's current context, through the driver entry point
+// (the library links only the CUDA runtime, so it loads where no driver is)
+static int current_context_id(unsigned long long* id) {
+  using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+  static CtxGetId fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !f)
+      return fail(CTGB_ERR_CUDA, std::string("cuCtxGetId entry point: ") + cudaGetErrorString(e));
+    fn = reinterpret_cast<CtxGetId>(f);
+  }
+  const CUresult r = fn(nullptr, id);
+  if (r != CUDA_SUCCESS) return fail(CTGB_ERR_CUDA, "cuCtxGetId failed with driver error " + std::to_string((int)r));
+  return CTGB_OK;
+}
 
 // Device address of the scratch array on `device`, which must be current.
 static int noalloc_scratch(int device, void** out) {
   if (device < 0 || device >= 256) return fail(CTGB_ERR_INVALID, "device index out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_dev_ptr[device]) {
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc != CTGB_OK) return rc;
+  NoAllocEntry& ent = g_noalloc_dev[device];
+  if (ent.ctx_id != ctx || !ent.ptr) {
     void* ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
       return fail(CTGB_ERR_CUDA, std::string("scratch symbol address: ") + cudaGetErrorString(e));
-    g_noalloc_dev_ptr[device] = ptr;
+    ent.ptr = ptr;
+    ent.ctx_id = ctx;
   }
-  *out = g_noalloc_dev_ptr[device];
+  *out = ent.ptr;
   return CTGB_OK;
 }
 
@@ -1760,8 +1791,11 @@ static int projection_noalloc(const ctgb_plan* p, const void* image, void* sino,
   if (cur != p->device) CTGB_CUDA(cudaSetDevice(p->device));
   void* ws = nullptr;
   int rc = noalloc_scratch(p->device, &ws);
-  // The layout kernel rewrites every scratch element the gather reads (zero
-  // padding included), so nothing left by an earlier call needs clearing.
+  // Nothing left in the array by an earlier call (possibly of another plan,
+  // with other line lengths) needs clearing: the layout kernel writes every
+  // element the detector gather reads, and the gather clamps its pixel index
+  // to N - 1, so it never reads the padding columns of a line (round8(N) - N
+  // of them), which the layout kernel leaves as they were.
   if (rc == CTGB_OK) rc = dispatch(p, CTGB_OP_PROJECTION, image, sino, batch, ws, kNoAllocScratchBytes, stream);
   if (cur != p->device && cur >= 0) cudaSetDevice(cur);
   return rc;

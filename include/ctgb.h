@@ -167,10 +167,13 @@ int ctgb_data_gradient(const ctgb_plan* plan, const void* image, const void* sin
  * static scratch array of ctgb_projection_noalloc_max_bytes() bytes (64 MiB)
  * inside this library, reserved on every GPU that loads it until process exit.
  * A batch whose scratch (ctgb_workspace_size for CTGB_OP_PROJECTION) exceeds
- * that size fails with CTGB_ERR_WORKSPACE. The first call on a device looks up
- * the array's device address; make that first call before any stream capture.
- * All calls share the one array: calls whose work overlaps on the GPU (other
- * streams, other threads) race on it and must be serialised by the caller. */
+ * that size fails with CTGB_ERR_WORKSPACE. The first call on a device (and the
+ * first after its context is destroyed and created again, e.g. by
+ * cudaDeviceReset) looks up the array's device address; make that first call
+ * before any stream capture. All calls share the one array, which keeps the
+ * last call's contents (nothing in it needs clearing between calls): calls
+ * whose work overlaps on the GPU (other streams, other threads) race on it and
+ * must be serialised by the caller. */
 int ctgb_projection_noalloc(const ctgb_plan* plan, const void* image, void* sino, int batch, void* stream);
 
 /* Size in bytes of the static scratch array used by ctgb_projection_noalloc. */

@@ -47,7 +47,7 @@ def _load_oracle():
 
 
 def ref_available() -> bool:
-    return os.path.exists(_build.REF_SO) or os.path.isdir(os.path.join(_build.DEFAULT_REF_ROOT, "src"))
+    return os.path.exists(_build.REF_SO) or _build.ref_root() is not None
 
 
 def _load_ref():

@@ -48,7 +48,20 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "libctref.so")
+# The CTLIB checkout whose kernels these recipes compile: $CTLIB_REF_ROOT when
+# set, else the read-only mount of the build container. Where neither exists
+# (a machine that only runs the prebuilt files), build_ref and build_ref_gpu
+# return None and the tests that need them skip.
+REF_ROOT_ENV = "CTLIB_REF_ROOT"
 DEFAULT_REF_ROOT = "/root/reference"
+
+
+def ref_root() -> str | None:
+    """The checkout to build from, or None when there is none."""
+    for cand in (os.environ.get(REF_ROOT_ENV), DEFAULT_REF_ROOT):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
 
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off"]
 
@@ -94,9 +107,12 @@ def _kernel_text(path: str) -> str:
     return text
 
 
-def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | None:
+def build_ref(root: str | None = None, force: bool = False) -> str | None:
     """Compile the reference kernels for CPU execution; None if no checkout."""
-    srcdir = os.path.join(ref_root, "src")
+    root = root or ref_root()
+    if root is None:
+        return None
+    srcdir = os.path.join(root, "src")
     if not os.path.isdir(srcdir):
         return None
     deps = [os.path.join(srcdir, f) for _, f in _KERNEL_FILES]
@@ -178,12 +194,15 @@ _REF_NVCC = ["-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17
              "--expt-relaxed-constexpr", "-DTORCH_EXTENSION_NAME=ctlib", "-DTORCH_API_INCLUDE_EXTENSION_H"]
 
 
-def build_ref_gpu(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> list[str] | None:
+def build_ref_gpu(root: str | None = None, force: bool = False) -> list[str] | None:
     """Compile the reference kernels to compressed sm_103a cubins; None if no checkout."""
     import gzip
     import shutil
     import sysconfig
-    srcdir = os.path.join(ref_root, "src")
+    root = root or ref_root()
+    if root is None:
+        return None
+    srcdir = os.path.join(root, "src")
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.isdir(srcdir) or not os.path.exists(nvcc):
         return None

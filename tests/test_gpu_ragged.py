@@ -73,3 +73,27 @@ def test_ragged_graph_replay(env, branches):
             ot = torch.tensor(o, dtype=torch.float32)
             want = ct.fbp(ct.projection(x * (1.0 + trial), ot), ot)
             assert torch.equal(y, want)
+
+
+@pytest.mark.parametrize("branches", [0, 2])
+def test_ragged_graph_outlives_batch(env, branches):
+    """The replay callable keeps alive everything its kernels read: after the
+    RaggedBatch object itself is dropped and collected (and fresh allocations
+    reuse freed memory), replays still give the per-slice results."""
+    import gc
+    ct, batched = env
+    opts = _slices()
+    from ctlib_gb300.workloads import ellipse_phantom
+    imgs = [torch.from_numpy(ellipse_phantom(int(o[3]), int(o[2]), o[4], 90 + i)[None, None]).cuda()
+            for i, o in enumerate(opts)]
+    rb = batched.RaggedBatch(opts)
+    replay, static_in, outs = rb.graphed(("projection", "fbp"), imgs, branches=branches)
+    del rb
+    gc.collect()
+    junk = [torch.full((1 << 18,), 3.0, device="cuda") for _ in range(32)]
+    replay()
+    torch.cuda.synchronize()
+    del junk
+    for x, o, y in zip(imgs, opts, outs):
+        ot = torch.tensor(o, dtype=torch.float32)
+        assert torch.equal(y, ct.fbp(ct.projection(x, ot), ot))
