@@ -706,6 +706,175 @@ def run_ragged(args):
     return 0
 
 
+def run_unrolled(args):
+    """Unrolled reconstruction: one step = K gradient-descent iterations
+    x <- x - a A^T(A x - y) from x = 0 on the whole batch, each iteration
+    checkpointed, then backpropagation of 0.5 ||x_K - x_true||^2 to the
+    measured sinogram y (y.grad). y is Poisson log data of the phantoms
+    (I0 = 1e5, counts clamped >= 1, seed 11) and a = 1 / lambda_max(A^T A).
+    Ray-updates are counted over the operator launches one step actually makes
+    (counted on an untimed step). Our arm runs ctlib_gb300.recon.unrolled_gd;
+    --impl reference runs the same recursion through torch autograd on the
+    reference's own kernels (oracle/ref_cuda.py), and the CPU port's rate on a
+    bounded sample."""
+    import torch
+
+    import ctlib_gb300 as ctlib
+    from ctlib_gb300 import autograd as ag
+    from ctlib_gb300 import recon
+    from ctlib_gb300.workloads import WORKLOADS, phantoms
+
+    ws, rank, local = _dist()
+    if args.impl == "reference" and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]()
+    B = len(w.slices)
+    o = w.slices[0].options
+    V, D, W, H = (int(o[i]) for i in range(4))
+    opts = torch.tensor(o, dtype=torch.float32)
+    x_true_h = torch.from_numpy(np.stack(phantoms(w))[:, None]).contiguous()
+    xt = x_true_h.to(dev)
+    y_h = torch.from_numpy(recon.poisson_log_sinogram(ctlib.projection(xt, opts).cpu().numpy(), 1e5, 11))
+    y_dev = y_h.to(dev)
+    step_a = recon.gd_step_size(opts, H, W, dev)
+    K = args.unrolled
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    if args.impl == "reference":
+        from oracle import ref_cuda
+        if not ref_cuda.available():
+            print(json.dumps({"impl": "reference", "unavailable": "reference cubins not built"}), flush=True)
+            return 0
+        ref = ref_cuda.get()
+        od = torch.tensor(o, dtype=torch.float32, device=dev)
+
+        class _RefLinear(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, x, fwd, bwd):
+                ctx.bwd = bwd
+                return ref.run(fwd, x.detach().contiguous(), od)
+
+            @staticmethod
+            def backward(ctx, g):
+                return ref.run(ctx.bwd, g.contiguous(), od), None, None
+
+        A = lambda x: _RefLinear.apply(x, 0, 1)
+        At = lambda s: _RefLinear.apply(s, 1, 0)
+        counted = ref_cuda.RefCuda.run
+    else:
+        A = lambda x: ag.projection(x, opts)
+        At = lambda s: ag.projection_t(s, opts)
+        counted = None
+
+    from torch.utils.checkpoint import checkpoint
+
+    def one_iter(x, y):
+        return x - step_a * At(A(x) - y)
+
+    def forward_backward(y):
+        y = y.detach().requires_grad_(True)
+        if args.impl == "reference":
+            x = torch.zeros_like(xt)
+            for _ in range(K):
+                x = checkpoint(one_iter, x, y, use_reentrant=False)
+        else:
+            x = recon.unrolled_gd(y, opts, K, step_a)
+        loss = 0.5 * ((x - xt) ** 2).sum()
+        loss.backward()
+        return loss.detach(), y.grad
+
+    # operator launches per step, counted on one untimed step
+    calls = [0]
+    if counted is None:
+        orig = ag._run
+
+        def counting(op, x, plan):
+            calls[0] += 1
+            return orig(op, x, plan)
+        ag._run = counting
+        try:
+            forward_backward(y_dev)
+        finally:
+            ag._run = orig
+    else:
+        orig = ref_cuda.RefCuda.run
+
+        def counting(self, op, *a, **k):
+            calls[0] += 1
+            return orig(self, op, *a, **k)
+        ref_cuda.RefCuda.run = counting
+        try:
+            forward_backward(y_dev)
+        finally:
+            ref_cuda.RefCuda.run = orig
+    ops_per_step = calls[0]
+    ru_step = ops_per_step * w.ray_updates()
+
+    for _ in range(args.warmup):
+        forward_backward(y_dev)
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    clk = ClockSampler(local)
+    clk.start()
+    ms = timed(lambda: forward_backward(y_dev))
+    clocks = clk.stop()
+    # end to end: measured sinogram from pinned host memory, gradient and loss back
+    y_pin = y_h.pin_memory()
+    g_h = torch.empty_like(y_h).pin_memory()
+    l_h = torch.empty((), dtype=torch.float32).pin_memory()
+
+    def e2e():
+        loss, g = forward_backward(y_pin.to(dev, non_blocking=True))
+        g_h.copy_(g, non_blocking=True)
+        l_h.copy_(loss, non_blocking=True)
+
+    e2e()
+    e2e_ms = timed(e2e)
+    value = ru_step / (ms / 1e3)
+    line = {"metric": f"ray-updates/s unrolled GD ({K} it, checkpointed) fwd+bwd {w.name}", "value": value,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic ellipse phantoms (seeded), Poisson log data I0=1e5 seed 11",
+            "config": {"workload": w.name, "global_batch": B, "views": V, "dets": D, "image": [H, W],
+                       "iterations": K, "step_size": step_a, "operator_launches_per_step": ops_per_step,
+                       "ray_updates_per_step": ru_step, "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": ru_step / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(y_h.numel() * 4), "d2h_bytes_per_step": int(y_h.numel() * 4 + 4)},
+            "clocks": clocks}
+    if args.impl == "reference":
+        line["impl"] = "reference"
+        line["path"] = ("torch autograd over the reference's prj_fan_ea / prj_t_fan_ea kernels compiled for "
+                        "sm_103a (oracle/ref_cuda.py), the same checkpointed recursion")
+    else:
+        line["path"] = "ctlib_gb300.recon.unrolled_gd through ctlib_gb300.autograd (projection <-> projection_t)"
+        # each operator call launches a layout kernel and a gather kernel
+        line["gpu_launches"] = 2 * ops_per_step * args.steps
+        peak = _fp32_peak(dev)
+        model_peak = peak["lane_ops_per_s"] / 8.0
+        line["roofline_fp32"] = {"achieved": value, "peak": model_peak, "unit": "ray-updates/s",
+                                 "frac": value / model_peak, "scope": "whole step (all operator launches)",
+                                 "model": "8 FP32 lane-ops per ray-update at measured FFMA lane-op rate",
+                                 "peak_source": "builder-measured FFMA rate (ctlib_gb300/csrc/peak_fp32.cu)"}
+        line["cpu_baseline"] = _cpu_baseline(w)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def _kernel_times(plan, steps, flush, stream, run_a, run_at):
     """Mean durations (ms) of the gather kernel of projection and of
     projection_t alone: the library records caller events right around each
@@ -781,6 +950,8 @@ def main():
                     help="time each operator of the API alone on the workload (both arms)")
     ap.add_argument("--batch", type=int, default=0, help="with --operators: slices per call (default: the workload's)")
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"], help="with --operators: element type")
+    ap.add_argument("--unrolled", type=int, default=0,
+                    help="time K checkpointed gradient-descent iterations forward + backward (both arms)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
@@ -788,6 +959,8 @@ def main():
         return run_laplacian_only(args)
     if args.operators:
         return run_operators(args)
+    if args.unrolled:
+        return run_unrolled(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload.startswith("ragged"):

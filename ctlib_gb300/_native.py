@@ -80,6 +80,10 @@ def _declare(l):
     l.ctgb_plan_set_schedule.restype = c_int
     l.ctgb_plan_set_unroll.argtypes = [vp, c_int, c_int]
     l.ctgb_plan_set_unroll.restype = c_int
+    l.ctgb_plan_set_wait_limit.argtypes = [vp, ctypes.c_ulonglong]
+    l.ctgb_plan_set_wait_limit.restype = c_int
+    l.ctgb_plan_set_summation.argtypes = [vp, c_int]
+    l.ctgb_plan_set_summation.restype = c_int
     l.ctgb_plan_set_filter.argtypes = [vp, c_int, c_int]
     l.ctgb_plan_set_filter.restype = c_int
     l.ctgb_plan_set_kernel_events.argtypes = [vp, vp, vp]
@@ -149,6 +153,7 @@ def check(rc: int, what: str):
 
 
 EXPORTED = ("ctgb_plan_create", "ctgb_plan_destroy", "ctgb_plan_info", "ctgb_plan_set_schedule", "ctgb_plan_set_unroll", "ctgb_plan_set_filter",
+            "ctgb_plan_set_summation", "ctgb_plan_set_wait_limit",
             "ctgb_plan_set_kernel_events",
             "ctgb_workspace_size",
             "ctgb_projection", "ctgb_projection_t", "ctgb_backprojection", "ctgb_backprojection_t",

@@ -76,6 +76,7 @@ struct DevPlan {
   int V, D, W, H, L, scan;
   int Dp;             // D rounded up to a multiple of 4: row stride of cell records and sinogram planes
   int even_taps;      // fbp filter with non-zero even offsets (windowed kernels), besides the centre
+  unsigned long long wait_ns;  // limit of each bounded wait in the staged image gather
   T dImg, s2r, dAng, wscale;
   const int* flags;   // V
   const T* src;       // V*2   source x, y
@@ -354,7 +355,7 @@ struct ResidualOut {
   T* q;
 };
 
-template <class T, int SB, int KIND, int U, bool RES = false>
+template <class T, int SB, int KIND, int U, bool RES = false, bool PLAIN = false>
 __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int d, int g, const T* __restrict__ imx,
                                                 const T* __restrict__ imy, size_t sx_line, size_t sy_line,
                                                 T* __restrict__ out, int B, ResidualOut<T> ro = {}) {
@@ -408,7 +409,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
       k = 0;
     }
     if (k >= N || b <= T(0)) {
-      if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
+      if (!PLAIN && (l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
       continue;
     }
     // pixels past the line's end take no weight: with b clamped to N - k their
@@ -469,7 +470,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
         for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(w, u[i], blk[qd * QW + i]);
       }
     }
-    if ((l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
+    if (!PLAIN && (l % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
   }
   kahan_fold_smem<T, SB>(acc, blk, blockDim.x);
   T fac = T(1);
@@ -510,7 +511,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
 template <class T, int U>
 constexpr int det_max_regs() { return (sizeof(T) == 4 && U == 2) ? 96 : 72; }
 
-template <class T, int SB, int KIND, int U, bool RES = false>
+template <class T, int SB, int KIND, int U, bool RES = false, bool PLAIN = false>
 __global__ void __maxnreg__((det_max_regs<T, U>())) k_det_gather(DevPlan<T> P, const T* __restrict__ imx,
                                                     const T* __restrict__ imy, T* __restrict__ out, int B,
                                                     ResidualOut<T> ro) {
@@ -518,16 +519,20 @@ __global__ void __maxnreg__((det_max_regs<T, U>())) k_det_gather(DevPlan<T> P, c
   const int d = blockIdx.x * 32 + lane;
   const int v = blockIdx.y * (blockDim.x >> 5) + warp;
   if (v >= P.V || d >= P.D) return;
-  det_gather_cell<T, SB, KIND, U, RES>(P, v, d, blockIdx.z, imx, imy, (size_t)round8(P.W) * SB,
+  det_gather_cell<T, SB, KIND, U, RES, PLAIN>(P, v, d, blockIdx.z, imx, imy, (size_t)round8(P.W) * SB,
                                        (size_t)round8(P.H) * SB, out, B, ro);
 }
 
 // ----------------------------------------------------------------------------
 // mbarrier and bulk-copy primitives (PTX, sm_90 and later)
 // ----------------------------------------------------------------------------
-// Every wait is bounded: after kWaitLimitNs of polling it gives up, the kernel
-// counts the event in g_wait_timeouts and falls back to global loads, so a
-// stalled copy can never hang the GPU.
+// Every wait is bounded: after the plan's wait limit (DevPlan::wait_ns, 1 s by
+// default) of polling it gives up, the kernel counts the event in
+// g_wait_timeouts and falls back to global loads, so a stalled copy can never
+// hang the GPU. A limit of 0 makes a wait give up unless its phase has already
+// completed at the first try (ctgb_plan_set_wait_limit: the fallback path on
+// demand, for tests). The producer's final drain of copies in flight always
+// allows kWaitLimitNs, whatever the plan's limit.
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
 __device__ unsigned long long g_wait_timeouts;
 
@@ -565,13 +570,14 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 // wait for the completion of the phase of parity `parity`; false if it did not
-// complete within the limit
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// complete within `limit_ns` (0: only the first try)
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
+  if (limit_ns == 0) return false;
   const unsigned long long t0 = global_ns();
   for (unsigned i = 1; i < (1u << 30); ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) break;
+    if ((i & 255u) == 0 && global_ns() - t0 > limit_ns) break;
   }
   return false;
 }
@@ -836,7 +842,7 @@ struct PixSlot {
 // is the same in either order, so the result is deterministic. SV writes every
 // view's image directly, so it takes any number of parts. Shorter CTAs fill the
 // last wave of a grid that is only a few waves deep.
-template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1>
+template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1, bool PLAIN = false>
 __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, int B, T out_mul, T out_div,
                                                        int nsplit) {
@@ -934,19 +940,35 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
     int ws, l0 = 0, nl = 0;
     load_in(vbeg + lane, cur);
     ws = window(vbeg + lane, cur, l0, nl);
+    // Views issued so far (header written and the slot's full barrier armed).
+    // Before use u of a slot the producer waits until the consumers released
+    // use u - 1 (empty) and until use u - 1's copies landed (full), so at most
+    // one phase of each full barrier is ever pending. Once a wait has run out
+    // (here or in a consumer, s_bad), the producer issues nothing more: no
+    // header, arrive or copy, since an arrive on a phase still waiting for its
+    // bytes would exceed that phase's expected count.
+    int issued = 0;
     for (int ub = 0; ub < NV; ub += 32) {
       load_in(vbeg + ub + 32 + lane, nxt);  // in flight during this batch's copies
       const int nv = min(32, NV - ub);
-      for (int j = 0; j < nv; ++j) {
+      int j = 0;
+      for (; j < nv; ++j) {
         const int vj = vbeg + ub + j, slot = (ub + j) % kSlots, use = (ub + j) / kSlots;
-        if (lane == 0 && use > 0 && !ld_volatile(s_bad)) {
-          if (!mbar_wait(&s_empty[slot], (use - 1) & 1)) report_timeout(&s_bad);
+        int go = 1;
+        if (lane == 0) {
+          if (ld_volatile(s_bad)) {
+            go = 0;
+          } else if (use > 0 && !(mbar_wait(&s_empty[slot], (use - 1) & 1, P.wait_ns) &&
+                                  mbar_wait(&s_full[slot], (use - 1) & 1, P.wait_ns))) {
+            report_timeout(&s_bad);
+            go = 0;
+          }
         }
-        __syncwarp();
+        if (!__shfl_sync(0xffffffffu, go, 0)) break;
         const int wsj = __shfl_sync(0xffffffffu, ws, j);
         const int l0j = __shfl_sync(0xffffffffu, l0, j);
         const int nlj = __shfl_sync(0xffffffffu, nl, j);
-        const bool staged = wsj >= 0 && !ld_volatile(s_bad);
+        const bool staged = wsj >= 0;
         if (lane == j) {
           s_hdr[slot][0] = make_int4(staged ? ws : -1, cur.fl, l0, __float_as_int(cur.sd.a));
           s_hdr[slot][1] = make_int4(__float_as_int(cur.sd.b), __float_as_int(cur.sd.c), __float_as_int(cur.sd.d),
@@ -955,6 +977,7 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
           s_src[slot][1] = cur.sy;
         }
         __syncwarp();
+        ++issued;
         if (!staged) {
           if (lane == 0) mbar_arrive(&s_full[slot]);
           continue;
@@ -974,15 +997,24 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         else if (lane == NQ + 1)
           bulk_g2s(sl + S::kQBytes + S::kRecBytes, P.lp + ((size_t)vj * P.L + l0j) * 4, lbytes, &s_full[slot]);
       }
+      if (j < nv) break;  // stopped after a timeout
       cur = nxt;
       ws = window(vbeg + ub + 32 + lane, cur, l0, nl);
     }
-    // Normally the consumers have waited on every phase issued. After a wait
-    // ran out, make sure no copy is still landing in this CTA's shared memory.
+    // Normally the consumers wait on every phase issued. After a timeout, wait
+    // for the last issued phase of every slot (the only one that can still be
+    // pending), so that no copy is still landing in this CTA's shared memory
+    // when the producer returns; this drain always allows kWaitLimitNs. A copy
+    // is issued only with in-bounds source and destination (window start
+    // clamped to [0, Dp), byte counts from the copied range), so on a working
+    // GPU it lands within microseconds and the drain ends at once. Should the
+    // drain itself run out, the event is counted once more and the producer
+    // returns; the consumers finish on global loads, and a copy still in flight
+    // could then land in shared memory that a later CTA on the same SM owns.
     if (lane == 0 && ld_volatile(s_bad)) {
-      for (int i = 0; i < kSlots && i < NV; ++i) {
-        const int last = i + ((NV - 1 - i) / kSlots) * kSlots;
-        mbar_wait(&s_full[i], (last / kSlots) & 1);
+      for (int i = 0; i < kSlots && i < issued; ++i) {
+        const int last = i + ((issued - 1 - i) / kSlots) * kSlots;
+        if (!mbar_wait(&s_full[i], (last / kSlots) & 1, kWaitLimitNs)) report_timeout(&s_bad);
       }
     }
     return;
@@ -1013,7 +1045,7 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
     const int v = vbeg + u, slot = u % kSlots;
     bool ok = false;
     if (!ld_volatile(s_bad)) {
-      ok = mbar_wait(&s_full[slot], (u / kSlots) & 1);
+      ok = mbar_wait(&s_full[slot], (u / kSlots) & 1, P.wait_ns);
       if (!ok) report_timeout(&s_bad);
     }
     if (SV) {
@@ -1062,7 +1094,7 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
           if (bb < B) img[(((size_t)bb * V + v) * P.H + rp[p]) * P.W + c] = blk[p][s];
         }
       }
-    } else if ((u % kFoldEvery) == kFoldEvery - 1) {
+    } else if (!PLAIN && (u % kFoldEvery) == kFoldEvery - 1) {
 #pragma unroll
       for (int p = 0; p < PX; ++p) kahan_fold_smem<T, SB>(acc + (size_t)p * 2 * SB * CT, blk[p], CT);
     }
@@ -1121,7 +1153,7 @@ __device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int 
 // ----------------------------------------------------------------------------
 // Called by every thread of the CTA; `smem` holds 4D + SB*D elements. In fp32
 // the taps are pairs (taps, tapl) and the low parts are summed separately.
-template <class T, int SB>
+template <class T, int SB, bool PLAIN = false>
 __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int g, const T* __restrict__ y,
                                                  T* __restrict__ q, int qs, int B, T* smem) {
   constexpr bool kLo = sizeof(T) == 4;
@@ -1195,7 +1227,7 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
         const bool ok = ti >= 0 && ti < 2 * D - 1;
         win[0] = ok ? taps[ti] : T(0);
         wlo[0] = ok ? tapl[ti] : T(0);
-        if ((step & 15) == 15) {
+        if (!PLAIN && (step & 15) == 15) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const T y = sub_rn(part[i], comp[i]);
@@ -1231,11 +1263,11 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
   }
 }
 
-template <class T, int SB>
+template <class T, int SB, bool PLAIN = false>
 __global__ void __launch_bounds__(256) k_ramp_filter(DevPlan<T> P, const T* __restrict__ y, T* __restrict__ q,
                                                      int B) {
   extern __shared__ unsigned char smem_raw[];
-  ramp_filter_view<T, SB>(P, blockIdx.x, blockIdx.y, y, q, P.Dp, B, reinterpret_cast<T*>(smem_raw));
+  ramp_filter_view<T, SB, PLAIN>(P, blockIdx.x, blockIdx.y, y, q, P.Dp, B, reinterpret_cast<T*>(smem_raw));
 }
 
 // ----------------------------------------------------------------------------
@@ -1254,6 +1286,9 @@ struct ctgb_plan {
   // straight-line steps of the gather loop (3 or 2; 2 is built for fp32 with
   // 4 or more slices per thread, other widths always use 3)
   int unroll[6] = {3, 3, 3, 3, 3, 3};
+  // one plain fp32 running sum per output instead of compensated sums
+  // (ctgb_plan_set_summation; fp32 plans, the five operators only)
+  bool plain = false;
   // optional events recorded right before and after each gather kernel on the
   // launch stream (ctgb_plan_set_kernel_events), to time that kernel alone
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
@@ -1338,6 +1373,7 @@ static int upload(ctgb_plan* p) {
   P.tapl = reinterpret_cast<const T*>(b + offs[12]);
   P.rec = reinterpret_cast<const T*>(b + offs[13]);
   P.Dp = Dp;
+  P.wait_ns = kWaitLimitNs;
   P.flags = reinterpret_cast<const int*>(b + off_flags);
   P.inv = reinterpret_cast<const float*>(b + off_inv);
   if constexpr (sizeof(T) == 4) p->pf = P; else p->pd = P;
@@ -1369,6 +1405,12 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
 // two straight-line steps are instantiated for the widths that carry batches
 template <class T, int SB>
 constexpr bool kTwoStep = sizeof(T) == 4 && SB >= 4;
+
+// plain-summation variants (no Kahan folds) are instantiated for fp32 with three
+// straight-line steps only: they serve error studies, not speed; for fp64 the
+// flag names the default kernels, so no extra fp64 code is built
+template <class T>
+constexpr bool kPlainBuilt = sizeof(T) == 4;
 
 // bytes of the image line planes of the detector gather, and of the sinogram
 // planes of the image gather, for G slice groups of SB slices
@@ -1424,11 +1466,14 @@ static int launch_det(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
     kern<<<grid, 32 * wpc, acc_smem, st>>>(P, imx, imy, y, batch, ro);
     if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
   };
+  const bool plain = !RES && kPlainBuilt<T> && p->plain;
   if (RES || op == CTGB_OP_PROJECTION) {
-    if (two) launch(k_det_gather<T, SB, kA, U2, RES>);
+    if (plain) launch(k_det_gather<T, SB, kA, 3, false, kPlainBuilt<T>>);
+    else if (two) launch(k_det_gather<T, SB, kA, U2, RES>);
     else launch(k_det_gather<T, SB, kA, 3, RES>);
   } else {
-    if (two) launch(k_det_gather<T, SB, kBt, U2>);
+    if (plain) launch(k_det_gather<T, SB, kBt, 3, false, kPlainBuilt<T>>);
+    else if (two) launch(k_det_gather<T, SB, kBt, U2>);
     else launch(k_det_gather<T, SB, kBt, 3>);
   }
   return CTGB_OK;
@@ -1442,14 +1487,15 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
                       T* qb, bool planes_ready, cudaStream_t st) {
   const int G = (batch + SB - 1) / SB;
   const HostGeom& g = p->geom;
+  const bool plain = kPlainBuilt<T> && p->plain && op != CTGB_OP_BACKPROJECTION_SV;
   if (!planes_ready && op == CTGB_OP_FBP) {
     const size_t smem = ((size_t)4 * g.D + (size_t)SB * g.D) * sizeof(T);
+    auto ramp = plain ? k_ramp_filter<T, SB, kPlainBuilt<T>> : k_ramp_filter<T, SB>;
     if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(k_ramp_filter<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(ramp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ramp filter smem: ") + cudaGetErrorString(e));
     }
-    k_ramp_filter<T, SB><<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
+    ramp<<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
   } else if (!planes_ready) {
     const int tb = 256;
     const int nb = (int)std::min<size_t>((size_t)G * g.V * Planes<SB>::NQ, 152 * 16);
@@ -1485,6 +1531,12 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   };
   constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
   const bool two = kTwoStep<T, SB> && p->unroll[sched] == 2;
+  constexpr bool PL = kPlainBuilt<T>;
+  if (plain) {
+    if (op == CTGB_OP_PROJECTION_T) return launch(k_pix_gather<T, SB, kAt, 3, false, PX, PL>, T(1), T(1));
+    if (op == CTGB_OP_BACKPROJECTION) return launch(k_pix_gather<T, SB, kB, 3, false, PX, PL>, T(1), T(1));
+    return launch(k_pix_gather<T, SB, kB, 3, false, PX, PL>, P.dAng, T(2));
+  }
   if (op == CTGB_OP_BACKPROJECTION_SV)
     return two ? launch(k_pix_gather<T, SB, kB, U2, true, PX>, T(1), T(1))
                : launch(k_pix_gather<T, SB, kB, 3, true, PX>, T(1), T(1));
@@ -2081,6 +2133,23 @@ int ctgb_plan_set_filter(ctgb_plan* plan, int window, int ea_exact) {
   plan->geom.taps = g2.taps;
   plan->geom.taps_lo = g2.taps_lo;
   plan->pf.even_taps = plan->pd.even_taps = window != kRamLak;
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_wait_limit(ctgb_plan* plan, unsigned long long limit_ns) {
+  if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
+  if (limit_ns > 10 * ctgb::kWaitLimitNs)
+    return ctgb::fail(CTGB_ERR_INVALID, "wait limit above 10 s; the default is 1 s");
+  plan->pf.wait_ns = plan->pd.wait_ns = limit_ns;
+  return CTGB_OK;
+}
+
+int ctgb_plan_set_summation(ctgb_plan* plan, int compensated) {
+  if (!plan) return ctgb::fail(CTGB_ERR_INVALID, "null plan");
+  if (compensated != 0 && compensated != 1) return ctgb::fail(CTGB_ERR_INVALID, "compensated must be 0 or 1");
+  if (!compensated && plan->dtype != CTGB_FLOAT32)
+    return ctgb::fail(CTGB_ERR_INVALID, "plain summation is offered for float32 plans only");
+  plan->plain = !compensated;
   return CTGB_OK;
 }
 

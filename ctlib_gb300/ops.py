@@ -59,6 +59,12 @@ class Plan:
                 pass
             self.handle = None
 
+    def set_summation(self, compensated: bool):
+        """Compensated (default) or one plain fp32 running sum per output
+        (ctgb_plan_set_summation). Plans from ``get_plan`` are shared: change
+        this only on a plan of your own (``Plan(values, dtype, device)``)."""
+        N.check(N.lib().ctgb_plan_set_summation(self.handle, int(bool(compensated))), "summation")
+
     def workspace_bytes(self, op: int, batch: int) -> int:
         return int(N.lib().ctgb_workspace_size(self.handle, op, batch))
 

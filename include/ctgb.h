@@ -77,6 +77,28 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
  * in the reference (its merge walk has no fixed step count). */
 int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps);
 
+/* Limit, in nanoseconds, of every bounded wait in the staged image gather
+ * (projection_t, backprojection, fbp, backprojection_sv) on this plan:
+ * 1000000000 (1 s) by default, at most 10 s. A wait that runs out makes its
+ * CTA finish on global loads, with the same results, and is counted by
+ * ctgb_wait_timeouts. 0 makes every wait give up unless its copy has already
+ * landed at the first look, which takes the fallback path on purpose (for
+ * tests of it). No counterpart in the reference, whose kernels do not wait. */
+int ctgb_plan_set_wait_limit(ctgb_plan* plan, unsigned long long limit_ns);
+
+/* Summation order of one plan's operators: compensated = 1 (the default) sums
+ * each output's terms over lines (projection, backprojection_t), views
+ * (projection_t, backprojection, fbp) and filter taps (fbp) in plain fp32
+ * blocks of 32 (16 taps) folded into a Kahan-compensated total; compensated = 0
+ * keeps one plain fp32 running sum per output instead, as the reference's walk
+ * does (src/fan_ed_kernel.cu:360-401 accumulates each pixel and bin straight
+ * into an fp32 value). The plain form exists to measure what compensation
+ * buys: float32 plans only (CTGB_ERR_INVALID for float64), applied by the five
+ * operators (ctgb_data_gradient and ragged batches always compensate), with
+ * three straight-line steps whatever the schedule. Results of either form do
+ * not depend on the schedule. No counterpart in the reference. */
+int ctgb_plan_set_summation(ctgb_plan* plan, int compensated);
+
 /* Ramp filter of fbp on this plan: window 0 = Ram-Lak (the reference's kernel,
  * the default), 1 = Shepp-Logan, 2 = Ram-Lak under a Hann window; ea_exact != 0
  * (equal-angle fans only) scales each tap by (n dDet / sin(n dDet))^2, which
@@ -152,7 +174,12 @@ int ctgb_backprojection_sv(const ctgb_plan* plan, const void* sino, void* images
  * CTGB_OP_PROJECTION (its first kernel) and CTGB_OP_PROJECTION_T (its second);
  * workspace: ctgb_workspace_size(plan, CTGB_OP_DATA_GRADIENT, batch). No single
  * counterpart in the reference: a caller composes it from projection and
- * projection_t (src/ctlib.cpp:56-84). */
+ * projection_t (src/ctlib.cpp:56-84).
+ * A convenience entry with no speed claim: it runs the same two gathers as the
+ * composed calls, and on the 16-slice 512^2 fan-ED batch it takes the same time
+ * (5.30 against 5.29 ms). What fusion saves is the subtraction pass and the
+ * sinogram re-layout, about 0.1 GB of memory traffic (tens of microseconds);
+ * the two gathers, bound by their instruction issue, are the other 99%. */
 int ctgb_data_gradient(const ctgb_plan* plan, const void* image, const void* sino, void* residual, void* grad,
                        int batch, void* workspace, size_t workspace_bytes, void* stream);
 

@@ -1,7 +1,10 @@
 """Autograd pairs: each operator's backward is its hand-written adjoint.
 
-* gradcheck in fp64 (finite differences vs the adjoint kernel) on a 64x64 crop
-  of the fan equal-distance geometry;
+* gradcheck in fp64 (the full finite-difference Jacobian vs the adjoint
+  kernel) on 64x64 crops of the fan equal-distance, equal-angle and parallel
+  geometries, for all four operators;
+* the fp32 dot-product test <Ax,y> = <x,A^T y> on the full fan-ED, fan-EA and
+  parallel benchmark geometries;
 * an unrolled 10-iteration gradient-descent reconstruction x <- x - a*A^T(Ax - y)
   on equal-angle fan geometry with per-iteration activation checkpointing; the
   gradient of the final loss with respect to the measured sinogram is checked
@@ -36,18 +39,97 @@ def _crop_geometry(scan=0):
     return fan_options(48, 72, 64, 64, 0.7, 0.0011, 0.1, 2 * math.pi / 48, 541.0, 408.0, 0.0, FAN_EA)
 
 
+def _crop_parallel():
+    from ctlib_gb300.workloads import para_options
+    return para_options(48, 72, 64, 64, 1.0, 1.3, 0.1, math.pi / 48, 0.2)
+
+
+def _geometry_table(opts, what):
+    """Host geometry table `what` of ctgb_geometry_query, in fp64."""
+    import ctypes
+    from ctlib_gb300 import _native as N
+    l = N.lib()
+    o = (ctypes.c_double * len(opts))(*opts)
+    n = l.ctgb_geometry_query(o, len(opts), 1, what, None, 0)
+    assert n > 0, N.last_error()
+    out = (ctypes.c_double * n)()
+    l.ctgb_geometry_query(o, len(opts), 1, what, out, n)
+    return np.frombuffer(out, dtype=np.float64).copy()
+
+
+def ea_bt_factor(opts):
+    """Per sinogram element (view, external bin) the factor dImg / cbar by which
+    the reference's equal-angle backprojection_t exceeds the transpose of its
+    backprojection (src/fan_ea_kernel.cu:590-607): fq * cell width, fq being
+    the projection's dImg / (cbar * width), mapped from increasing-boundary
+    order to the sinogram's bin order of each view."""
+    V, D = int(opts[0]), int(opts[1])
+    flags = _geometry_table(opts, 0).astype(np.int64)
+    db = _geometry_table(opts, 1).reshape(V, D + 1)
+    fq = _geometry_table(opts, 2).reshape(V, D)
+    f = fq * np.diff(db, axis=1)
+    flip = (flags & 2) != 0
+    f[flip] = f[flip, ::-1]
+    return f
+
+
+GEOMETRIES = {"fan_ed": lambda: _crop_geometry(0), "fan_ea": lambda: _crop_geometry(1), "parallel": _crop_parallel}
+
+
+@pytest.mark.parametrize("geom", sorted(GEOMETRIES))
 @pytest.mark.parametrize("which", ["projection", "projection_t", "backprojection", "backprojection_t"])
-def test_gradcheck_fp64(ag, which):
-    opts = torch.tensor(_crop_geometry(), dtype=torch.float64)
+def test_gradcheck_fp64(ag, geom, which):
+    """Full finite-difference Jacobian (not a random projection of it) against
+    the Jacobian the hand-written adjoint kernel gives, in fp64 on a 64 x 64
+    crop, 48 views x 72 bins. For equal-angle fans the backprojector pair is
+    the reference's, whose backprojection_t carries an extra dImg / cbar per
+    (view, bin): there the check runs on the pair with that factor divided out
+    of the adjoint, which makes it the exact transpose (the factor itself is
+    ea_bt_factor, from the plan's geometry tables)."""
+    opts_l = GEOMETRIES[geom]()
+    opts = torch.tensor(opts_l, dtype=torch.float64)
     g = torch.Generator().manual_seed(3)
-    if which in ("projection", "backprojection_t"):
-        x = torch.randn(1, 1, 64, 64, generator=g, dtype=torch.float64)
-    else:
-        x = torch.randn(1, 1, 48, 72, generator=g, dtype=torch.float64)
-    x = x.cuda().requires_grad_(True)
+    img_in = which in ("projection", "backprojection_t")
+    shape = (1, 1, 64, 64) if img_in else (1, 1, 48, 72)
+    x = torch.randn(shape, generator=g, dtype=torch.float64).cuda().requires_grad_(True)
     fn = getattr(ag, which)
+    if geom == "fan_ea" and which in ("backprojection", "backprojection_t"):
+        q3 = torch.from_numpy(ea_bt_factor(opts_l)).view(1, 1, 48, 72).cuda()
+        if which == "backprojection":
+            # f = B; its autograd gradient is the reference's backprojection_t,
+            # q3 * B^T g, and a hook divides q3 back out before it reaches t
+            def f(t):
+                t2 = t * 1.0
+                t2.register_hook(lambda gr: gr / q3)
+                return ag.backprojection(t2, opts)
+        else:
+            # f = backprojection_t / q3 = B^T; the gradient reaching the
+            # operator's output is g / q3, which a hook turns back into g, so
+            # the operator's backward (backprojection) gives B g
+            def f(t):
+                out = ag.backprojection_t(t, opts)
+                out.register_hook(lambda gr: gr * q3)
+                return out / q3
+        assert torch.autograd.gradcheck(f, (x,), eps=1e-6, atol=1e-8, rtol=1e-6, fast_mode=False)
+        return
     assert torch.autograd.gradcheck(lambda t: fn(t, opts), (x,), eps=1e-6, atol=1e-8, rtol=1e-6,
-                                    fast_mode=True)
+                                    fast_mode=False)
+
+
+def test_ea_backprojector_pair_factor(ag):
+    """Equal-angle backprojection_t is exactly q3 times the transpose of
+    backprojection (fp64 dot products): <B y, x> = <y, backprojection_t(x) / q3>,
+    while without the division the identity fails by the factor's spread."""
+    opts_l = _crop_geometry(1)
+    opts = torch.tensor(opts_l, dtype=torch.float64)
+    g = torch.Generator().manual_seed(9)
+    x = torch.randn(2, 1, 64, 64, generator=g, dtype=torch.float64).cuda()
+    y = torch.randn(2, 1, 48, 72, generator=g, dtype=torch.float64).cuda()
+    q3 = torch.from_numpy(ea_bt_factor(opts_l)).view(1, 1, 48, 72).cuda()
+    lhs = float((ag.backprojection(y, opts) * x).sum())
+    bt = ag.backprojection_t(x, opts)
+    assert abs(lhs - float((y * bt / q3).sum())) <= 1e-11 * abs(lhs)
+    assert abs(lhs - float((y * bt).sum())) > 1e-3 * abs(lhs)
 
 
 def test_dot_product_fp32_headline_geometry(ag):
@@ -63,6 +145,25 @@ def test_dot_product_fp32_headline_geometry(ag):
     y = ag.projection(x2, o) + torch.randn(2, 1, 1152, 736, generator=g).cuda()
     lhs = float((ag.projection(x, o).double() * y.double()).sum())
     rhs = float((x.double() * ag.projection_t(y, o).double()).sum())
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), abs(lhs - rhs) / abs(lhs)
+
+
+@pytest.mark.parametrize("workload", ["fan_ea_512", "parallel_256"])
+def test_dot_product_fp32_full_geometries(ag, workload):
+    """The fp32 adjoint mismatch |<Ax,y> - <x,A^T y>| / |<Ax,y>| <= 1e-6 on the
+    full equal-angle (512^2, 984 views, 888 bins) and parallel (256^2, 360
+    views, 367 bins) geometries, inputs built as in the fan-ED test."""
+    from ctlib_gb300.workloads import WORKLOADS
+    o_l = WORKLOADS[workload]().slices[0].options
+    o = torch.tensor(o_l, dtype=torch.float32)
+    V, D, W, H = (int(o_l[i]) for i in range(4))
+    g = torch.Generator().manual_seed(7)
+    x = torch.randn(2, 1, H, W, generator=g).cuda()
+    x2 = x + 0.5 * torch.randn(2, 1, H, W, generator=g).cuda()
+    y = ag.projection(x2, o) + torch.randn(2, 1, V, D, generator=g).cuda()
+    lhs = float((ag.projection(x, o).double() * y.double()).sum())
+    rhs = float((x.double() * ag.projection_t(y, o).double()).sum())
+    print(f"{workload}: adjoint mismatch {abs(lhs - rhs) / abs(lhs):.2e}")
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs), abs(lhs - rhs) / abs(lhs)
 
 
