@@ -1,6 +1,6 @@
 """Ragged batches: slices with different geometries processed together.
 
-    rb = RaggedBatch([options_0, options_1, ...])      # one options vector per slice
+    rb = RaggedBatch([options_0, options_1, ...])      # one options vector per slice (fp32; dtype=torch.float64 too)
     sinos = rb.projection([img_0, img_1, ...])          # list of 1 x 1 x V_i x D_i
     recs = rb.fbp(sinos)                                 # list of 1 x 1 x H_i x W_i
 
@@ -32,12 +32,15 @@ _OPS = {"projection": N.OP_PROJECTION, "projection_t": N.OP_PROJECTION_T, "backp
 
 
 class RaggedBatch:
-    def __init__(self, options_list, device=None):
+    def __init__(self, options_list, device=None, dtype=torch.float32):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
+        if dtype not in (torch.float32, torch.float64):
+            raise ValueError(f"dtype must be float32 or float64, got {dtype}")
         self.device = torch.device(device)
+        self.dtype = dtype
         idx = self.device.index if self.device.index is not None else torch.cuda.current_device()
-        self.plans = [get_plan(o, torch.float32, self.device) for o in options_list]
+        self.plans = [get_plan(o, dtype, self.device) for o in options_list]
         n = len(self.plans)
         arr = (ctypes.c_void_p * n)(*[p.handle.value for p in self.plans])
         h = ctypes.c_void_p()
@@ -69,12 +72,12 @@ class RaggedBatch:
             raise ValueError(f"expected {self.n} slices, got {len(inputs)}")
         out_shapes, in_shapes = self._shapes(op)
         for i, (x, shp) in enumerate(zip(inputs, in_shapes)):
-            if not (x.is_cuda and x.is_contiguous() and x.dtype == torch.float32):
-                raise RuntimeError(f"slice {i}: input must be a contiguous float32 CUDA tensor")
+            if not (x.is_cuda and x.is_contiguous() and x.dtype == self.dtype):
+                raise RuntimeError(f"slice {i}: input must be a contiguous {self.dtype} CUDA tensor")
             if tuple(x.shape) != shp and x.numel() != shp[2] * shp[3]:
                 raise ValueError(f"slice {i}: input shape {tuple(x.shape)}, expected {shp}")
         if outputs is None:
-            outputs = [torch.empty(s, dtype=torch.float32, device=self.device) for s in out_shapes]
+            outputs = [torch.empty(s, dtype=self.dtype, device=self.device) for s in out_shapes]
         nbytes = self.workspace_bytes(op)
         if workspace is None:
             workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
@@ -119,7 +122,7 @@ class RaggedBatch:
         for name in ops:
             op = _OPS[name]
             out_shapes, _ = self._shapes(op)
-            outs = [torch.empty(s, dtype=torch.float32, device=self.device) for s in out_shapes]
+            outs = [torch.empty(s, dtype=self.dtype, device=self.device) for s in out_shapes]
             ws = torch.empty(max(self.workspace_bytes(op), 1), dtype=torch.uint8, device=self.device)
             bufs.append((op, cur, outs, ws))
             cur = outs
@@ -146,7 +149,7 @@ class RaggedBatch:
                 op = _OPS[name]
                 tune.apply_cached(plan, op, 1)  # the schedule a per-slice call would use
                 out_shapes, _ = self._shapes(op)
-                out = torch.empty(out_shapes[i], dtype=torch.float32, device=self.device)
+                out = torch.empty(out_shapes[i], dtype=self.dtype, device=self.device)
                 nbytes = plan.workspace_bytes(op, 1)
                 ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
                 chain.append((plan, op, cur, out, ws, nbytes))

@@ -674,10 +674,9 @@ struct CellSpan {
 // overlaps (cells past the pixel or the range get weight 0 on a clamped, valid
 // cell).
 template <class T, int KIND, int U, bool SM>
-__device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
+__device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, T kf, const Seed& sd, T sx, T sy,
                                          T pcx, T pcy, const T* __restrict__ rec, int base, int dlo, int dhi,
                                          CellSpan<T, U>& cs) {
-  const T kf = T(k);
   // x = alpha + sigma*k as (xs, xl)
   const T qh = mul_rn(A4.z, kf);
   const T ql = fma(A4.z, kf, -qh);
@@ -770,11 +769,11 @@ __device__ __forceinline__ void pix_accum(const CellSpan<T, U>& cs, const T* __r
 
 // one view's contribution to one pixel, accumulated into blk
 template <class T, int SB, int KIND, int U, bool SM>
-__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, int k, const Seed& sd, T sx, T sy,
+__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, T kf, const Seed& sd, T sx, T sy,
                                          T pcx, T pcy, const T* __restrict__ rec, const T* __restrict__ qv, int qs,
                                          int base, int dlo, int dhi, T (&blk)[SB]) {
   CellSpan<T, U> cs;
-  pix_geom<T, KIND, U, SM>(P, A4, k, sd, sx, sy, pcx, pcy, rec, base, dlo, dhi, cs);
+  pix_geom<T, KIND, U, SM>(P, A4, kf, sd, sx, sy, pcx, pcy, rec, base, dlo, dhi, cs);
   pix_accum<T, SB, KIND, U, SM>(cs, rec, qv, qs, base, dhi, blk);
 }
 
@@ -786,16 +785,20 @@ __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int 
   const bool xb = P.flags[v] & 1;
   const int k = xb ? c : P.H - 1 - r;
   const Quad<T> A4 = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r : c)) * 4);
-  pix_view<T, SB, KIND, U, false>(P, A4, k, load_seed(P.inv + (size_t)v * 5), P.src[2 * v], P.src[2 * v + 1], pcx,
+  pix_view<T, SB, KIND, U, false>(P, A4, T(k), load_seed(P.inv + (size_t)v * 5), P.src[2 * v], P.src[2 * v + 1], pcx,
                                   pcy, P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
 }
 
-// Parts per tile of the staged image gather: two view halves whenever there are
-// enough views. Halving every tile's CTA time fills the last wave of grids that
-// are only a few waves deep. The split depends on V alone, never on the launch
-// schedule, so every schedule still gives the same result bit for bit; the
-// ragged path sums the same halves and matches too.
-__host__ __device__ __forceinline__ int view_split(int views) { return views >= 64 ? 2 : 1; }
+// Parts per tile of the staged image gather: a tile's views are split into
+// consecutive parts of at least 128 views, up to 8, each part its own CTA.
+// Shorter CTAs fill the last wave of a grid that is only a few waves deep (one
+// 512^2 slice is 1024 tile halves, 2.2 waves of 456 resident CTAs; 16 slices
+// are 4.5 waves). Each part writes its scaled sum to its own partial image and
+// k_combine_parts adds the parts in order, from zero, so the result does not
+// depend on which CTA finishes first. The split depends on V alone, never on
+// the batch or the schedule, so every schedule gives the same result bit for
+// bit; the ragged path sums the same parts in the same order and matches too.
+__host__ __device__ __forceinline__ int view_split(int views) { return views < 256 ? 1 : (views >= 1024 ? 8 : views / 128); }
 
 // Staged image gather. A CTA is a 32 x (R * PX) pixel tile plus one producer
 // warp: R consumer warps, lane = column, and warp w owns rows w, w + R, ...,
@@ -837,15 +840,18 @@ struct PixSlot {
 // sum goes to its own image, img[slice][view][row][col], with no sum over views.
 //
 // nsplit: blockIdx.z = slice group * nsplit + part, and part p takes views
-// [V*p/nsplit, V*(p+1)/nsplit). Summing operators use 1 or 2 parts: with two,
-// each adds its scaled sum into the zeroed output with one atomic add; 0 + a + b
-// is the same in either order, so the result is deterministic. SV writes every
-// view's image directly, so it takes any number of parts. Shorter CTAs fill the
-// last wave of a grid that is only a few waves deep.
-template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1, bool PLAIN = false>
-__global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
-                                                       T* __restrict__ img, int B, T out_mul, T out_div,
-                                                       int nsplit) {
+// [V*p/nsplit, V*(p+1)/nsplit). Summing operators use view_split(V) parts:
+// with one, the CTA writes the output; with more, part p writes its scaled sum
+// to partial image p of `parts` ([nsplit][B][H][W]) and k_combine_parts adds
+// them. SV writes every view's image directly, so it takes any number of parts
+// and no partial images.
+//
+// The CTA's work, (bx, by, bz) standing for its block index: k_pix_gather runs
+// it over a regular grid, k_rag_pix_gather over a task list of several slices.
+template <class T, int SB, int KIND, int U, bool SV, int PX, bool PLAIN>
+__device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __restrict__ q, T* __restrict__ img,
+                                               T* __restrict__ parts, int B, T out_mul, T out_div, int nsplit,
+                                               int bx, int by, int bz) {
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
   constexpr int kWin = S::kWin;
@@ -862,8 +868,8 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   const int CT = 32 * R;                     // consumer threads
   T* acc = reinterpret_cast<T*>(pix_smem);  // [2][PX * SB][CT]: running sum, compensation
   unsigned char* slots = pix_smem + (size_t)2 * PX * SB * CT * sizeof(T);
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * R * PX;
-  const int part = blockIdx.z % nsplit, g = blockIdx.z / nsplit;
+  const int c0 = bx * 32, r0 = by * R * PX;
+  const int part = bz % nsplit, g = bz / nsplit;
   const int V = P.V, D = P.D, Dp = P.Dp;
   const int vbeg = (int)((long long)V * part / nsplit), vend = (int)((long long)V * (part + 1) / nsplit);
   const int NV = vend - vbeg;  // views of this CTA; the slot of view vbeg + u is u % kSlots
@@ -970,8 +976,12 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         const int nlj = __shfl_sync(0xffffffffu, nl, j);
         const bool staged = wsj >= 0;
         if (lane == j) {
-          s_hdr[slot][0] = make_int4(staged ? ws : -1, cur.fl, l0, __float_as_int(cur.sd.a));
-          s_hdr[slot][1] = make_int4(__float_as_int(cur.sd.b), __float_as_int(cur.sd.c), __float_as_int(cur.sd.d),
+          // staged: the window's cell count and the seed shifted to window-relative
+          // cells, so that consumers index the slot directly (the seed only starts
+          // the search for the bracketing cell, so its rounding never matters)
+          s_hdr[slot][0] = make_int4(staged ? min(kWin, D - ws) : -1, cur.fl, l0, __float_as_int(cur.sd.a));
+          s_hdr[slot][1] = make_int4(__float_as_int(cur.sd.b), __float_as_int(cur.sd.c),
+                                     __float_as_int(staged ? cur.sd.d - (float)ws : cur.sd.d),
                                      __float_as_int(cur.sd.e));
           s_src[slot][0] = cur.sx;
           s_src[slot][1] = cur.sy;
@@ -1024,11 +1034,12 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
   const int c = c0 + lane;
   int rp[PX];
   bool act[PX];
-  T pcy[PX];
+  T pcy[PX], kf_row[PX];
   bool any = false;
 #pragma unroll
   for (int p = 0; p < PX; ++p) {
     rp[p] = r0 + warp + p * R;
+    kf_row[p] = T(P.H - 1 - rp[p]);
     act[p] = c < P.W && rp[p] < P.H;
     pcy[p] = act[p] ? P.rowc[rp[p]] : T(0);
     any = any || act[p];
@@ -1041,11 +1052,14 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
 #pragma unroll
     for (int s = 0; s < SB; ++s) blk[p][s] = T(0);
   }
+  const T kf_col = T(c);  // the pixel's edge index on row lines; on column lines it is H - 1 - r
+  int slot = 0;
+  unsigned phase = 0;
   for (int u = 0; u < NV; ++u) {
-    const int v = vbeg + u, slot = u % kSlots;
+    const int v = vbeg + u;
     bool ok = false;
     if (!ld_volatile(s_bad)) {
-      ok = mbar_wait(&s_full[slot], (u / kSlots) & 1, P.wait_ns);
+      ok = mbar_wait(&s_full[slot], phase, P.wait_ns);
       if (!ok) report_timeout(&s_bad);
     }
     if (SV) {
@@ -1071,8 +1085,8 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         for (int p = 0; p < PX; ++p) {
           if (PX > 1 && !act[p]) continue;
           const Quad<T> A4 = ldrec<T, true>(slp + ((xb ? rp[p] : c) - h0.z) * 4);
-          pix_view<T, SB, KIND, U, true>(P, A4, xb ? c : P.H - 1 - rp[p], sd, sx, sy, pcx, pcy[p], srec, sq, kWin,
-                                         h0.x, h0.x, min(h0.x + kWin, D), blk[p]);
+          pix_view<T, SB, KIND, U, true>(P, A4, xb ? kf_col : kf_row[p], sd, sx, sy, pcx, pcy[p], srec, sq, kWin,
+                                         0, 0, h0.x, blk[p]);
         }
       } else {
 #pragma unroll
@@ -1084,6 +1098,10 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&s_empty[slot]);
+    if (++slot == kSlots) {
+      slot = 0;
+      phase ^= 1u;
+    }
     if (SV) {
 #pragma unroll
       for (int p = 0; p < PX; ++p) {
@@ -1110,39 +1128,49 @@ __global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __
         const int bb = g * SB + s;
         if (bb >= B) continue;
         const T val = ap[(size_t)s * CT + threadIdx.x] * out_mul / out_div;
-        T* dst = img + ((size_t)bb * P.H + rp[p]) * P.W + c;
-        if (nsplit == 1) *dst = val;
-        else atomicAdd(dst, val);
+        T* base = nsplit == 1 ? img : parts + (size_t)part * B * P.H * P.W;
+        base[((size_t)bb * P.H + rp[p]) * P.W + c] = val;
       }
     }
   }
 }
 
-// Unstaged image gather over one pixel per thread, one slice (ragged batches:
-// sinogram rows [V][D], no padding); called by every thread of the CTA.
-template <class T, int KIND>
-__device__ __forceinline__ void pix_gather_tile_global(const DevPlan<T>& P, int c, int r, const T* __restrict__ q,
-                                                       T* __restrict__ img, T out_mul, T out_div) {
-  extern __shared__ unsigned char pix_smem_g[];
-  T* acc = reinterpret_cast<T*>(pix_smem_g);
-  const bool active = c < P.W && r < P.H;
-  if (!active) return;
-  const T pcx = P.colc[c], pcy = P.rowc[r];
-  // the same view parts, fold points and final additions as k_pix_gather
-  const int nsplit = view_split(P.V);
-  T out = T(0);
-  for (int part = 0; part < nsplit; ++part) {
-    const int vbeg = (int)((long long)P.V * part / nsplit), vend = (int)((long long)P.V * (part + 1) / nsplit);
-    kahan_init_smem<T, 1>(acc, blockDim.x);
-    T blk[1] = {T(0)};
-    for (int v = vbeg; v < vend; ++v) {
-      pix_view_global<T, 1, KIND, 3>(P, v, r, c, q + (size_t)v * P.D, P.D, pcx, pcy, blk);
-      if (((v - vbeg) % kFoldEvery) == kFoldEvery - 1) kahan_fold_smem<T, 1>(acc, blk, blockDim.x);
+template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1, bool PLAIN = false>
+__global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
+                                                       T* __restrict__ img, T* __restrict__ parts, int B,
+                                                       T out_mul, T out_div, int nsplit) {
+  pix_gather_cta<T, SB, KIND, U, SV, PX, PLAIN>(P, q, img, parts, B, out_mul, out_div, nsplit, blockIdx.x, blockIdx.y,
+                                                blockIdx.z);
+}
+
+// Sum of the view parts of the staged image gather: out[i] = ((0 + p_0[i]) +
+// p_1[i]) + ..., in part order (the order the ragged path adds its parts in).
+template <class T>
+__global__ void __launch_bounds__(256) k_combine_parts(const T* __restrict__ parts, T* __restrict__ out, size_t n,
+                                                       int nparts) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if constexpr (sizeof(T) == 4) {
+    if ((n & 3) == 0) {
+      const size_t n4 = n / 4;
+      const float4* p4 = reinterpret_cast<const float4*>(parts);
+      float4* o4 = reinterpret_cast<float4*>(out);
+      for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int p = 0; p < nparts; ++p) {
+          const float4 v = __ldcs(p4 + (size_t)p * n4 + i);
+          s.x = __fadd_rn(s.x, v.x); s.y = __fadd_rn(s.y, v.y);
+          s.z = __fadd_rn(s.z, v.z); s.w = __fadd_rn(s.w, v.w);
+        }
+        o4[i] = s;
+      }
+      return;
     }
-    kahan_fold_smem<T, 1>(acc, blk, blockDim.x);
-    out += acc[threadIdx.x] * out_mul / out_div;
   }
-  img[(size_t)r * P.W + c] = out;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    T s = T(0);
+    for (int p = 0; p < nparts; ++p) s = add_rn(s, parts[(size_t)p * n + i]);
+    out[i] = s;
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -1391,6 +1419,14 @@ static int slices_per_thread(int dtype, int batch, int tuned_cap = 0) {
 
 static size_t esize(int dtype) { return dtype == 0 ? 4 : 8; }
 
+// partial images of the staged image gather's view parts (none for one part
+// or for single-view backprojection, which writes each view's image directly)
+static size_t pix_parts_bytes(const HostGeom& g, int op, int batch, size_t es) {
+  const int np = view_split(g.V);
+  if (np == 1 || op == CTGB_OP_BACKPROJECTION_SV) return 0;
+  return ((size_t)np * batch * g.H * g.W * es + 255) & ~(size_t)255;
+}
+
 static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   const HostGeom& g = p->geom;
   const int sb = slices_per_thread(p->dtype, batch, p->sb_cap[op]);
@@ -1399,7 +1435,7 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
     return al(G * g.H * (size_t)round8(g.W) * sb * es) + al(G * g.W * (size_t)round8(g.H) * sb * es);
-  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
+  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es) + pix_parts_bytes(g, op, batch, es);
 }
 
 // two straight-line steps are instantiated for the widths that carry batches
@@ -1431,7 +1467,8 @@ static int gradient_sb(const ctgb_plan* p, int batch) {
 static size_t gradient_workspace_bytes(const ctgb_plan* p, int batch) {
   const int sb = gradient_sb(p, batch);
   const size_t G = (size_t)((batch + sb - 1) / sb);
-  return det_planes_bytes(p->geom, G, sb, esize(p->dtype)) + pix_planes_bytes(p->geom, G, sb, esize(p->dtype));
+  return det_planes_bytes(p->geom, G, sb, esize(p->dtype)) + pix_planes_bytes(p->geom, G, sb, esize(p->dtype)) +
+         pix_parts_bytes(p->geom, CTGB_OP_PROJECTION_T, batch, esize(p->dtype));
 }
 
 // Image re-layout + detector gather: A or B^T of x into y, or (RES) A's residual
@@ -1481,10 +1518,11 @@ static int launch_det(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
 
 // Staged image gather (A^T, B, fbp's backprojection, single-view B) from the
 // sinogram planes qb; unless `planes_ready`, qb is first filled from x (re-layout,
-// or the ramp filter for fbp).
+// or the ramp filter for fbp). `parts` holds the partial images of the view
+// parts (pix_parts_bytes), which k_combine_parts sums into y.
 template <class T, int SB>
 static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, const T* x, T* y, int batch,
-                      T* qb, bool planes_ready, cudaStream_t st) {
+                      T* qb, T* parts, bool planes_ready, cudaStream_t st) {
   const int G = (batch + SB - 1) / SB;
   const HostGeom& g = p->geom;
   const bool plain = kPlainBuilt<T> && p->plain && op != CTGB_OP_BACKPROJECTION_SV;
@@ -1519,14 +1557,16 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
     // single-view backprojection writes each view's image on its own, so its views
     // split over any number of CTAs with no adds: 8 parts shorten the CTAs of a
     // grid that is only ~2 waves deep (7.62 to 6.85 ms for 16 x 512^2, 1152 views)
-    const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? std::min(8, g.V) : view_split(g.V);
-    if (nsplit > 1 && op != CTGB_OP_BACKPROJECTION_SV) {
-      e = cudaMemsetAsync(y, 0, (size_t)batch * g.H * g.W * sizeof(T), st);
-      if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather clear: ") + cudaGetErrorString(e));
-    }
+    const bool sv = op == CTGB_OP_BACKPROJECTION_SV;
+    const int nsplit = sv ? std::min(8, g.V) : view_split(g.V);
     if (p->ev_start) cudaEventRecord(p->ev_start, st);
-    kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, batch, mul, div, nsplit);
+    kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, parts, batch, mul, div, nsplit);
     if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
+    if (nsplit > 1 && !sv) {
+      const size_t n = (size_t)batch * g.H * g.W;
+      const int cb = (int)std::min<size_t>((n / 4 + 255) / 256, 152 * 8);
+      k_combine_parts<T><<<std::max(cb, 1), 256, 0, st>>>(parts, y, n, nsplit);
+    }
     return CTGB_OK;
   };
   constexpr int U2 = kTwoStep<T, SB> ? 2 : 3;
@@ -1559,7 +1599,10 @@ static int run_op(const ctgb_plan* p, const DevPlan<T>& P, int op, const void* i
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
     rc = launch_det<T, SB, false>(p, P, op, op, x, y, batch, ws, st);
   else
-    rc = launch_pix<T, SB>(p, P, op, op, x, y, batch, static_cast<T*>(ws), false, st);
+    rc = launch_pix<T, SB>(p, P, op, op, x, y, batch, static_cast<T*>(ws),
+                           reinterpret_cast<T*>(static_cast<unsigned char*>(ws) +
+                                                pix_planes_bytes(p->geom, (batch + SB - 1) / SB, SB, sizeof(T))),
+                           false, st);
   if (rc != CTGB_OK) return rc;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -1574,11 +1617,15 @@ template <class T, int SB>
 static int run_gradient(const ctgb_plan* p, const DevPlan<T>& P, const T* x, const T* y, T* res, T* grad, int batch,
                         void* ws, cudaStream_t st) {
   const size_t G = (size_t)((batch + SB - 1) / SB);
-  T* qb = reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + det_planes_bytes(p->geom, G, SB, sizeof(T)));
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  const size_t det_b = det_planes_bytes(p->geom, G, SB, sizeof(T));
+  T* qb = reinterpret_cast<T*>(w + det_b);
+  T* parts = reinterpret_cast<T*>(w + det_b + pix_planes_bytes(p->geom, G, SB, sizeof(T)));
   int rc = launch_det<T, SB, true>(p, P, CTGB_OP_PROJECTION, CTGB_OP_PROJECTION, x, nullptr, batch, ws, st,
                                    ResidualOut<T>{y, res, qb});
   if (rc == CTGB_OK)
-    rc = launch_pix<T, SB>(p, P, CTGB_OP_PROJECTION_T, CTGB_OP_PROJECTION_T, nullptr, grad, batch, qb, true, st);
+    rc = launch_pix<T, SB>(p, P, CTGB_OP_PROJECTION_T, CTGB_OP_PROJECTION_T, nullptr, grad, batch, qb, parts, true,
+                           st);
   if (rc != CTGB_OK) return rc;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -1675,29 +1722,50 @@ static int dispatch_gradient(const ctgb_plan* p, const void* image, const void* 
 // thread, and a slice's row lines are its own image (no re-layout needed).
 constexpr int kMaxRagged = 128;
 
+template <class T>
 struct RaggedIO {
-  const float* in[kMaxRagged];
-  float* out[kMaxRagged];
+  const T* in[kMaxRagged];
+  T* out[kMaxRagged];
+};
+
+// every slice's device plan, passed by value as one kernel parameter (23.5 KB
+// for fp32 plans, 25.6 KB for fp64, of the 32 KB a launch may carry): a CTA
+// reads its slice's geometry from the constant bank, as a per-slice launch
+// reads its own plan
+template <class T>
+struct RaggedPlans {
+  DevPlan<T> p[kMaxRagged];
 };
 
 struct RTask {
   int slice, a, b;
 };
 
-__global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<float>* __restrict__ plans,
-                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+// one CTA of the staged image gather: tile column bx, tile row by, view part
+struct RPixTask {
+  int slice, bx, by, part;
+};
+
+// tile rows per CTA of the ragged image gather: 8 row warps, two pixel rows each
+// (the per-slice calls' layout for one slice per thread with 8 warps)
+constexpr int kRagPixWarps = 8;
+constexpr int kRagPixRows = kRagPixWarps * kPixRows<1>;
+
+template <class T>
+__global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<T>* __restrict__ plans,
+                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
                                                        unsigned char* ws, const size_t* __restrict__ off) {
-  __shared__ float tile[32][33];
+  __shared__ T tile[32][33];
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
     const int H = plans[tk.slice].H, W = plans[tk.slice].W;
-    const float* img = io.in[tk.slice];
-    float* imy = reinterpret_cast<float*>(ws + off[tk.slice]);
+    const T* img = io.in[tk.slice];
+    T* imy = reinterpret_cast<T*>(ws + off[tk.slice]);
     const int r0 = tk.a * 32, c0 = tk.b * 32;
     __syncthreads();
     for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
       const int rr = i >> 5, cc = i & 31, r = r0 + rr, c = c0 + cc;
-      tile[rr][cc] = (r < H && c < W) ? img[(size_t)r * W + c] : 0.f;
+      tile[rr][cc] = (r < H && c < W) ? img[(size_t)r * W + c] : T(0);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
@@ -1707,65 +1775,94 @@ __global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<float>* __r
   }
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<float>* __restrict__ plans,
-                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+template <class T, int KIND>
+__global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<T>* __restrict__ plans,
+                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
                                                         unsigned char* ws, const size_t* __restrict__ off) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<float> P = plans[tk.slice];
+    const DevPlan<T> P = plans[tk.slice];
     const int v = tk.a * (blockDim.x >> 5) + warp, d = tk.b * 32 + lane;
     if (v < P.V && d < P.D)
-      det_gather_cell<float, 1, KIND, 3>(P, v, d, 0, io.in[tk.slice],
-                                      reinterpret_cast<const float*>(ws + off[tk.slice]), (size_t)P.W,
-                                      (size_t)P.H, io.out[tk.slice], 1);
+      det_gather_cell<T, 1, KIND, 3>(P, v, d, 0, io.in[tk.slice], reinterpret_cast<const T*>(ws + off[tk.slice]),
+                                     (size_t)P.W, (size_t)P.H, io.out[tk.slice], 1);
   }
 }
 
-template <bool SCALE>
-__global__ void __launch_bounds__(256) k_rag_sino_rows(const DevPlan<float>* __restrict__ plans,
-                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+template <class T, bool SCALE>
+__global__ void __launch_bounds__(256) k_rag_sino_rows(const DevPlan<T>* __restrict__ plans,
+                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
                                                        unsigned char* ws, const size_t* __restrict__ off) {
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<float> P = plans[tk.slice];
+    const DevPlan<T> P = plans[tk.slice];
     const int v = tk.a, D = P.D;
     const bool flip = P.flags[v] & 2;
-    const float* y = io.in[tk.slice] + (size_t)v * D;
-    float* q = reinterpret_cast<float*>(ws + off[tk.slice]) + (size_t)v * D;
-    for (int d = threadIdx.x; d < D; d += blockDim.x) {
-      const float val = y[flip ? D - 1 - d : d];
-      q[d] = SCALE ? val * P.fq[(size_t)v * D + d] : val;
+    const T* y = io.in[tk.slice] + (size_t)v * D;
+    T* q = reinterpret_cast<T*>(ws + off[tk.slice]) + (size_t)v * P.Dp;
+    for (int d = threadIdx.x; d < P.Dp; d += blockDim.x) {
+      T val = T(0);
+      if (d < D) {
+        val = y[flip ? D - 1 - d : d];
+        if (SCALE) val *= P.fq[(size_t)v * D + d];
+      }
+      q[d] = val;
     }
   }
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(256) k_rag_pix_gather(const DevPlan<float>* __restrict__ plans,
-                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
-                                                        unsigned char* ws, const size_t* __restrict__ off,
-                                                        int fbp_scale) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// The staged image gather of k_pix_gather (one slice per thread, two pixel
+// rows, three straight-line cells), each CTA one task of the task list: the
+// same arithmetic, view parts and fold points as a per-slice call, so the
+// results are the same bit for bit. Sinogram planes [V][Dp] per slice at
+// off_q, partial images [parts][H][W] at off_parts.
+template <class T, int KIND>
+__global__ void __launch_bounds__(32 * (kRagPixWarps + 1), 3)
+    k_rag_pix_gather(const __grid_constant__ RaggedPlans<T> rp, const RPixTask* __restrict__ tasks,
+                     const __grid_constant__ RaggedIO<T> io, unsigned char* ws, const size_t* __restrict__ off_q,
+                     const size_t* __restrict__ off_parts, int fbp_scale) {
+  const RPixTask t = tasks[blockIdx.x];
+  const DevPlan<T>& P = rp.p[t.slice];
+  pix_gather_cta<T, 1, KIND, 3, false, kPixRows<1>, false>(
+      P, reinterpret_cast<const T*>(ws + off_q[t.slice]), io.out[t.slice],
+      reinterpret_cast<T*>(ws + off_parts[t.slice]), 1, fbp_scale ? P.dAng : T(1), fbp_scale ? T(2) : T(1),
+      view_split(P.V), t.bx, t.by, t.part);
+}
+
+// k_combine_parts over the slices whose views were split: task (slice, chunk
+// of kCombineChunk pixels)
+constexpr int kCombineChunk = 4096;
+template <class T>
+__global__ void __launch_bounds__(256) k_rag_combine(const __grid_constant__ RaggedPlans<T> rp,
+                                                     const RTask* __restrict__ tasks, int ntasks,
+                                                     const __grid_constant__ RaggedIO<T> io, unsigned char* ws,
+                                                     const size_t* __restrict__ off_parts) {
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<float> P = plans[tk.slice];
-    pix_gather_tile_global<float, KIND>(P, tk.b * 32 + lane, tk.a * (blockDim.x >> 5) + warp,
-                                        reinterpret_cast<const float*>(ws + off[tk.slice]), io.out[tk.slice],
-                                        fbp_scale ? P.dAng : 1.f, fbp_scale ? 2.f : 1.f);
-    __syncthreads();  // the next task's view staging reuses shared memory
+    const DevPlan<T>& P = rp.p[tk.slice];
+    const size_t n = (size_t)P.H * P.W;
+    const int np = view_split(P.V);
+    const T* parts = reinterpret_cast<const T*>(ws + off_parts[tk.slice]);
+    const size_t end = min(n, (size_t)(tk.a + 1) * kCombineChunk);
+    for (size_t i = (size_t)tk.a * kCombineChunk + threadIdx.x; i < end; i += blockDim.x) {
+      T s = T(0);
+      for (int p = 0; p < np; ++p) s = add_rn(s, parts[(size_t)p * n + i]);
+      io.out[tk.slice][i] = s;
+    }
   }
 }
 
-__global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<float>* __restrict__ plans,
-                                                  const RTask* __restrict__ tasks, int ntasks, RaggedIO io,
+template <class T>
+__global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<T>* __restrict__ plans,
+                                                  const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
                                                   unsigned char* ws, const size_t* __restrict__ off) {
   extern __shared__ unsigned char smem_raw[];
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<float> P = plans[tk.slice];
-    ramp_filter_view<float, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<float*>(ws + off[tk.slice]), P.D,
-                               1, reinterpret_cast<float*>(smem_raw));
+    const DevPlan<T> P = plans[tk.slice];
+    ramp_filter_view<T, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<T*>(ws + off[tk.slice]), P.Dp, 1,
+                           reinterpret_cast<T*>(smem_raw));
   }
 }
 
@@ -1854,7 +1951,7 @@ static int projection_noalloc(const ctgb_plan* p, const void* image, void* sino,
 }
 
 struct RaggedStage {
-  RTask* tasks = nullptr;  // device
+  const void* tasks = nullptr;  // device: RTask, or RPixTask for the image gather
   int n = 0;
   int grid = 0;
 };
@@ -1862,31 +1959,56 @@ struct RaggedStage {
 }  // namespace ctgb
 
 struct ctgb_ragged {
-  int n = 0, device = 0, maxD = 0;
+  int n = 0, device = 0, maxD = 0, dtype = 0;
   void* dev = nullptr;
-  const ctgb::DevPlan<float>* plans = nullptr;
-  const size_t* off_img = nullptr;   // per slice: transposed image in the workspace
-  const size_t* off_sino = nullptr;  // per slice: re-laid-out sinogram in the workspace
+  const void* plans = nullptr;  // device copy (DevPlan<T>[n]), for the kernels that walk a task list
+  void* host_plans = nullptr;   // the same plans (RaggedPlans<T>), passed by value to the image gather
+  const size_t* off_img = nullptr;    // per slice: transposed image in the workspace
+  const size_t* off_sino = nullptr;   // per slice: sinogram planes [V][Dp] in the workspace
+  const size_t* off_parts = nullptr;  // per slice: partial images of the view parts
   size_t ws_img = 0, ws_sino = 0;
-  ctgb::RaggedStage transpose, detg, rows, pixg, ramp;
+  size_t pix_smem = 0;
+  ctgb::RaggedStage transpose, detg, rows, pixg, ramp, combine;
 };
 
 namespace ctgb {
 
+template <class T>
+static const DevPlan<T>& plan_of(const ctgb_plan* p) {
+  if constexpr (sizeof(T) == 4) return p->pf; else return p->pd;
+}
+
+static void free_host_plans(ctgb_ragged* r) {
+  if (r->dtype == 0) delete static_cast<RaggedPlans<float>*>(r->host_plans);
+  else delete static_cast<RaggedPlans<double>*>(r->host_plans);
+  r->host_plans = nullptr;
+}
+
+template <class T>
 static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   int sms = 0;
   CTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r->device));
-  std::vector<DevPlan<float>> dp(n);
-  std::vector<size_t> oi(n), os(n);
+  std::vector<DevPlan<T>> dp(n);
+  std::vector<size_t> oi(n), os(n), opt(n);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  std::vector<std::pair<long, RTask>> tr, dg, rw, pg, rp;
+  // task lists, each entry with its length for the longest-first order
+  std::vector<std::pair<long, RTask>> tr, dg, rw, rp, cb;
+  std::vector<std::pair<long, RPixTask>> pg;
+  auto* hp = new RaggedPlans<T>();
+  r->host_plans = hp;
+  const size_t es = sizeof(T);
   for (int i = 0; i < n; ++i) {
     const HostGeom& g = plans[i]->geom;
-    dp[i] = plans[i]->pf;
+    dp[i] = plan_of<T>(plans[i]);
+    hp->p[i] = dp[i];
+    const int Dp = dp[i].Dp;
+    const int np = view_split(g.V);
     oi[i] = r->ws_img;
-    r->ws_img += al((size_t)g.H * g.W * sizeof(float));
+    r->ws_img += al((size_t)g.H * g.W * es);
     os[i] = r->ws_sino;
-    r->ws_sino += al((size_t)g.V * g.D * sizeof(float));
+    r->ws_sino += al((size_t)g.V * Dp * es);
+    opt[i] = r->ws_sino;
+    if (np > 1) r->ws_sino += al((size_t)np * g.H * g.W * es);
     if (g.D > r->maxD) r->maxD = g.D;
     const long lines = g.H > g.W ? g.H : g.W;
     for (int a = 0; a < (g.H + 31) / 32; ++a)
@@ -1897,59 +2019,122 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
       rw.push_back({g.D, {i, a, 0}});
       rp.push_back({(long)g.D * g.D, {i, a, 0}});
     }
-    for (int a = 0; a < (g.H + 7) / 8; ++a)
-      for (int b = 0; b < (g.W + 31) / 32; ++b) pg.push_back({g.V, {i, a, b}});
+    // a CTA's time grows with its views (a part's) and its pixels per thread
+    const long pix_len = (long)(g.V / np) * 64;
+    for (int part = 0; part < np; ++part)
+      for (int by = 0; by < (g.H + kRagPixRows - 1) / kRagPixRows; ++by)
+        for (int bx = 0; bx < (g.W + 31) / 32; ++bx) pg.push_back({pix_len, {i, bx, by, part}});
+    if (np > 1)
+      for (int a = 0; a < (int)(((size_t)g.H * g.W + kCombineChunk - 1) / kCombineChunk); ++a)
+        cb.push_back({np, {i, a, 0}});
   }
   // longest tasks first (stable, so a slice's tasks stay together)
-  for (auto* v : {&tr, &dg, &rw, &pg, &rp})
-    std::stable_sort(v->begin(), v->end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-  const size_t b_plans = al(sizeof(DevPlan<float>) * n), b_off = al(sizeof(size_t) * n);
-  const size_t b_tr = al(sizeof(RTask) * tr.size()), b_dg = al(sizeof(RTask) * dg.size()),
-               b_rw = al(sizeof(RTask) * rw.size()), b_pg = al(sizeof(RTask) * pg.size()),
-               b_rp = al(sizeof(RTask) * rp.size());
-  const size_t total = b_plans + 2 * b_off + b_tr + b_dg + b_rw + b_pg + b_rp;
+  auto by_len = [](const auto& x, const auto& y) { return x.first > y.first; };
+  for (auto* v : {&tr, &dg, &rw, &rp, &cb}) std::stable_sort(v->begin(), v->end(), by_len);
+  std::stable_sort(pg.begin(), pg.end(), by_len);
+  const size_t b_plans = al(sizeof(DevPlan<T>) * n), b_off = al(sizeof(size_t) * n);
+  std::vector<std::pair<std::vector<unsigned char>, size_t>> lists;  // bytes, entries
+  auto pack = [&](const auto& v) {
+    using E = typename std::decay_t<decltype(v)>::value_type::second_type;
+    std::vector<unsigned char> b(sizeof(E) * v.size());
+    for (size_t k = 0; k < v.size(); ++k) std::memcpy(b.data() + k * sizeof(E), &v[k].second, sizeof(E));
+    lists.push_back({std::move(b), v.size()});
+  };
+  pack(tr); pack(dg); pack(rw); pack(pg); pack(rp); pack(cb);
+  size_t total = b_plans + 3 * b_off;
+  for (auto& l : lists) total += al(l.first.size() ? l.first.size() : 1);
   std::vector<unsigned char> host(total, 0);
   size_t o = 0;
   auto put = [&](const void* src, size_t bytes, size_t span) {
-    std::memcpy(host.data() + o, src, bytes);
+    if (bytes) std::memcpy(host.data() + o, src, bytes);
     const size_t at = o;
     o += span;
     return at;
   };
-  std::vector<RTask> t;
-  const size_t o_plans = put(dp.data(), sizeof(DevPlan<float>) * n, b_plans);
+  const size_t o_plans = put(dp.data(), sizeof(DevPlan<T>) * n, b_plans);
   const size_t o_oi = put(oi.data(), sizeof(size_t) * n, b_off);
   const size_t o_os = put(os.data(), sizeof(size_t) * n, b_off);
-  size_t o_stage[5];
-  int cnt[5];
-  int k = 0;
-  for (auto* v : {&tr, &dg, &rw, &pg, &rp}) {
-    t.clear();
-    for (auto& e : *v) t.push_back(e.second);
-    const size_t span = k == 0 ? b_tr : k == 1 ? b_dg : k == 2 ? b_rw : k == 3 ? b_pg : b_rp;
-    o_stage[k] = put(t.data(), sizeof(RTask) * t.size(), span);
-    cnt[k] = (int)t.size();
-    ++k;
-  }
+  const size_t o_op = put(opt.data(), sizeof(size_t) * n, b_off);
+  size_t o_stage[6];
+  for (int k = 0; k < 6; ++k)
+    o_stage[k] = put(lists[k].first.data(), lists[k].first.size(), al(lists[k].first.size() ? lists[k].first.size() : 1));
   CTGB_CUDA(cudaMalloc(&r->dev, total));
   CTGB_CUDA(cudaMemcpy(r->dev, host.data(), total, cudaMemcpyHostToDevice));
   unsigned char* base = static_cast<unsigned char*>(r->dev);
-  r->plans = reinterpret_cast<const DevPlan<float>*>(base + o_plans);
+  r->plans = base + o_plans;
   r->off_img = reinterpret_cast<const size_t*>(base + o_oi);
   r->off_sino = reinterpret_cast<const size_t*>(base + o_os);
-  RaggedStage* st[5] = {&r->transpose, &r->detg, &r->rows, &r->pixg, &r->ramp};
-  const void* fns[5] = {(const void*)k_rag_transpose, (const void*)k_rag_det_gather<kA>,
-                        (const void*)k_rag_sino_rows<true>, (const void*)k_rag_pix_gather<kAt>,
-                        (const void*)k_rag_ramp};
-  for (int i = 0; i < 5; ++i) {
-    st[i]->tasks = reinterpret_cast<RTask*>(base + o_stage[i]);
-    st[i]->n = cnt[i];
+  r->off_parts = reinterpret_cast<const size_t*>(base + o_op);
+  RaggedStage* st[6] = {&r->transpose, &r->detg, &r->rows, &r->pixg, &r->ramp, &r->combine};
+  const void* fns[6] = {(const void*)k_rag_transpose<T>, (const void*)k_rag_det_gather<T, kA>,
+                        (const void*)k_rag_sino_rows<T, true>, nullptr, (const void*)k_rag_ramp<T>,
+                        (const void*)k_rag_combine<T>};
+  constexpr int kPX = kPixRows<1>;
+  r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots * PixSlot<T, 1>::kBytes;
+  for (const void* f : {(const void*)k_rag_pix_gather<T, kAt>, (const void*)k_rag_pix_gather<T, kB>})
+    CTGB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->pix_smem));
+  const size_t ramp_smem = (size_t)5 * r->maxD * es;
+  if (ramp_smem > 48 * 1024)
+    CTGB_CUDA(cudaFuncSetAttribute((const void*)k_rag_ramp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)ramp_smem));
+  for (int i = 0; i < 6; ++i) {
+    st[i]->tasks = base + o_stage[i];
+    st[i]->n = (int)lists[i].second;
+    if (i == 3) {  // image gather: one CTA per task
+      st[i]->grid = st[i]->n;
+      continue;
+    }
     int per_sm = 1;
-    const size_t smem = i == 4 ? (size_t)5 * r->maxD * sizeof(float)
-                               : (i == 1 || i == 3) ? (size_t)2 * 256 * sizeof(float) : 0;
+    const size_t smem = i == 4 ? ramp_smem : i == 1 ? (size_t)2 * 256 * es : 0;
     CTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 256, smem));
     const int cap = sms * (per_sm > 0 ? per_sm : 1);
-    st[i]->grid = cnt[i] < cap ? cnt[i] : cap;
+    st[i]->grid = st[i]->n < cap ? st[i]->n : cap;
+  }
+  return CTGB_OK;
+}
+
+template <class T>
+static int ragged_run_t(const ctgb_ragged* r, int op, const void* const* in, void* const* out, void* ws,
+                        void* stream) {
+  RaggedIO<T> io{};
+  for (int i = 0; i < r->n; ++i) {
+    if (!in[i] || !out[i]) return fail(CTGB_ERR_INVALID, "null slice pointer");
+    io.in[i] = static_cast<const T*>(in[i]);
+    io.out[i] = static_cast<T*>(out[i]);
+  }
+  const DevPlan<T>* plans = static_cast<const DevPlan<T>*>(r->plans);
+  const RaggedPlans<T>& hp = *static_cast<const RaggedPlans<T>*>(r->host_plans);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  auto rt = [](const RaggedStage& s) { return static_cast<const RTask*>(s.tasks); };
+  if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
+    k_rag_transpose<T><<<r->transpose.grid, 256, 0, st>>>(plans, rt(r->transpose), r->transpose.n, io, w,
+                                                          r->off_img);
+    const size_t acc_smem = (size_t)2 * 256 * sizeof(T);
+    if (op == CTGB_OP_PROJECTION)
+      k_rag_det_gather<T, kA><<<r->detg.grid, 256, acc_smem, st>>>(plans, rt(r->detg), r->detg.n, io, w,
+                                                                   r->off_img);
+    else
+      k_rag_det_gather<T, kBt><<<r->detg.grid, 256, acc_smem, st>>>(plans, rt(r->detg), r->detg.n, io, w,
+                                                                    r->off_img);
+  } else {
+    if (op == CTGB_OP_FBP) {
+      const size_t smem = (size_t)5 * r->maxD * sizeof(T);
+      k_rag_ramp<T><<<r->ramp.grid, 256, smem, st>>>(plans, rt(r->ramp), r->ramp.n, io, w, r->off_sino);
+    } else if (op == CTGB_OP_PROJECTION_T) {
+      k_rag_sino_rows<T, true><<<r->rows.grid, 256, 0, st>>>(plans, rt(r->rows), r->rows.n, io, w, r->off_sino);
+    } else {
+      k_rag_sino_rows<T, false><<<r->rows.grid, 256, 0, st>>>(plans, rt(r->rows), r->rows.n, io, w, r->off_sino);
+    }
+    const RPixTask* pt = static_cast<const RPixTask*>(r->pixg.tasks);
+    const int nt = 32 * (kRagPixWarps + 1);
+    if (op == CTGB_OP_PROJECTION_T)
+      k_rag_pix_gather<T, kAt><<<r->pixg.grid, nt, r->pix_smem, st>>>(hp, pt, io, w, r->off_sino, r->off_parts, 0);
+    else
+      k_rag_pix_gather<T, kB><<<r->pixg.grid, nt, r->pix_smem, st>>>(hp, pt, io, w, r->off_sino, r->off_parts,
+                                                                     op == CTGB_OP_FBP ? 1 : 0);
+    if (r->combine.n > 0)
+      k_rag_combine<T><<<r->combine.grid, 256, 0, st>>>(hp, rt(r->combine), r->combine.n, io, w, r->off_parts);
   }
   return CTGB_OK;
 }
@@ -1962,46 +2147,14 @@ static int ragged_run(const ctgb_ragged* r, int op, const void* const* in, void*
   const size_t need = (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) ? r->ws_img : r->ws_sino;
   if (!ws || wsb < need) return fail(CTGB_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
   if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) return fail(CTGB_ERR_INVALID, "workspace must be 256-byte aligned");
-  RaggedIO io{};
-  for (int i = 0; i < r->n; ++i) {
-    if (!in[i] || !out[i]) return fail(CTGB_ERR_INVALID, "null slice pointer");
-    io.in[i] = static_cast<const float*>(in[i]);
-    io.out[i] = static_cast<float*>(out[i]);
-  }
   int cur = -1;
   CTGB_CUDA(cudaGetDevice(&cur));
   if (cur != r->device) CTGB_CUDA(cudaSetDevice(r->device));
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  unsigned char* w = static_cast<unsigned char*>(ws);
-  if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
-    k_rag_transpose<<<r->transpose.grid, 256, 0, st>>>(r->plans, r->transpose.tasks, r->transpose.n, io, w,
-                                                       r->off_img);
-    const size_t acc_smem = (size_t)2 * 256 * sizeof(float);
-    if (op == CTGB_OP_PROJECTION)
-      k_rag_det_gather<kA><<<r->detg.grid, 256, acc_smem, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w,
-                                                                r->off_img);
-    else
-      k_rag_det_gather<kBt><<<r->detg.grid, 256, acc_smem, st>>>(r->plans, r->detg.tasks, r->detg.n, io, w,
-                                                                 r->off_img);
-  } else {
-    if (op == CTGB_OP_FBP) {
-      const size_t smem = (size_t)5 * r->maxD * sizeof(float);
-      k_rag_ramp<<<r->ramp.grid, 256, smem, st>>>(r->plans, r->ramp.tasks, r->ramp.n, io, w, r->off_sino);
-    } else if (op == CTGB_OP_PROJECTION_T) {
-      k_rag_sino_rows<true><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
-    } else {
-      k_rag_sino_rows<false><<<r->rows.grid, 256, 0, st>>>(r->plans, r->rows.tasks, r->rows.n, io, w, r->off_sino);
-    }
-    const size_t acc_smem = (size_t)2 * 256 * sizeof(float);
-    if (op == CTGB_OP_PROJECTION_T)
-      k_rag_pix_gather<kAt><<<r->pixg.grid, 256, acc_smem, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w,
-                                                                 r->off_sino, 0);
-    else
-      k_rag_pix_gather<kB><<<r->pixg.grid, 256, acc_smem, st>>>(r->plans, r->pixg.tasks, r->pixg.n, io, w,
-                                                                r->off_sino, op == CTGB_OP_FBP ? 1 : 0);
-  }
+  int rc = r->dtype == 0 ? ragged_run_t<float>(r, op, in, out, ws, stream)
+                         : ragged_run_t<double>(r, op, in, out, ws, stream);
   const cudaError_t e = cudaGetLastError();
   if (cur != r->device && cur >= 0) cudaSetDevice(cur);
+  if (rc != CTGB_OK) return rc;
   if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ragged launch: ") + cudaGetErrorString(e));
   return CTGB_OK;
 }
@@ -2208,19 +2361,22 @@ int ctgb_ragged_create(ctgb_ragged** ragged, const ctgb_plan* const* plans, int 
     return ctgb::fail(CTGB_ERR_INVALID, "ragged batches hold 1 to " + std::to_string(ctgb::kMaxRagged) + " slices");
   for (int i = 0; i < n_slices; ++i) {
     if (!plans[i]) return ctgb::fail(CTGB_ERR_INVALID, "null plan in ragged batch");
-    if (plans[i]->dtype != 0) return ctgb::fail(CTGB_ERR_INVALID, "ragged batches are float32");
+    if (plans[i]->dtype != plans[0]->dtype)
+      return ctgb::fail(CTGB_ERR_INVALID, "the plans of a ragged batch share one dtype");
     if (plans[i]->device != device) return ctgb::fail(CTGB_ERR_INVALID, "plan on another device");
   }
   auto* r = new ctgb_ragged();
   r->n = n_slices;
   r->device = device;
+  r->dtype = plans[0]->dtype;
   int cur = -1;
   cudaGetDevice(&cur);
   cudaSetDevice(device);
-  int rc = ctgb::ragged_build(r, plans, n_slices);
+  int rc = r->dtype == 0 ? ctgb::ragged_build<float>(r, plans, n_slices) : ctgb::ragged_build<double>(r, plans, n_slices);
   if (cur >= 0) cudaSetDevice(cur);
   if (rc != CTGB_OK) {
     if (r->dev) cudaFree(r->dev);
+    ctgb::free_host_plans(r);
     delete r;
     return rc;
   }
@@ -2231,6 +2387,7 @@ int ctgb_ragged_create(ctgb_ragged** ragged, const ctgb_plan* const* plans, int 
 int ctgb_ragged_destroy(ctgb_ragged* ragged) {
   if (!ragged) return CTGB_OK;
   if (ragged->dev) cudaFree(ragged->dev);
+  ctgb::free_host_plans(ragged);
   delete ragged;
   return CTGB_OK;
 }

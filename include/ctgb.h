@@ -206,9 +206,12 @@ int ctgb_projection_noalloc(const ctgb_plan* plan, const void* image, void* sino
 /* Size in bytes of the static scratch array used by ctgb_projection_noalloc. */
 size_t ctgb_projection_noalloc_max_bytes(void);
 
-/* Ragged batches: n slices (1..128), each with its own fp32 plan (image size,
- * views, detectors, geometry), processed together: every stage of an operator
- * is one persistent launch over a task list built here, longest tasks first.
+/* Ragged batches: n slices (1..128), each with its own plan (image size, views,
+ * detectors, geometry; all plans fp32 or all fp64), processed together: every
+ * stage of an operator is one launch over a task list built here, longest tasks
+ * first. The image gather's tasks are CTAs of the staged per-slice kernel (one
+ * per slice, pixel tile and view part), so the results equal per-slice calls
+ * bit for bit.
  * A run takes host arrays of n device pointers (slice i: 1 x 1 x H_i x W_i or
  * 1 x 1 x V_i x D_i) and needs no host-to-device copy, so it can be captured in
  * a CUDA graph. The plans must outlive the ragged object. No counterpart in the

@@ -1,5 +1,5 @@
-"""Ragged batches (one persistent launch per stage over slices of different
-geometries) must reproduce the per-slice calls exactly, directly and from a
+"""Ragged batches (one launch per stage over slices of different geometries,
+fp32 or fp64) must reproduce the per-slice calls exactly, directly and from a
 CUDA-graph replay."""
 
 import math
@@ -29,24 +29,43 @@ def _slices():
             fan_options(72, 91, 48, 40, 1.0, 0.008, 0.3, tp / 72, 120.0, 100.0, 0.01, FAN_EA),
             para_options(90, 67, 32, 48, 1.0, 1.1, 0.1, math.pi / 90, 0.4),
             para_options(12, 128, 96, 96, 1.0, 1.2, 0.0, math.pi / 12, 0.0),
-            fan_options(128, 256, 96, 80, 1.5, 2.5, 0.0, tp / 128, 595.0, 490.6, 0.0, FAN_ED)]
+            fan_options(128, 256, 96, 80, 1.5, 2.5, 0.0, tp / 128, 595.0, 490.6, 0.0, FAN_ED),
+            # enough views for the image gather to split them into parts (4 and 8),
+            # whose partial images a combine stage adds
+            fan_options(520, 180, 40, 56, 1.0, 2.0, 0.1, tp / 520, 150.0, 100.0, 0.2, FAN_ED),
+            para_options(1100, 80, 32, 32, 1.0, 1.0, 0.0, math.pi / 1100, 0.0)]
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("op", ["projection", "projection_t", "backprojection", "backprojection_t", "fbp"])
-def test_ragged_matches_per_slice_calls(env, op):
+def test_ragged_matches_per_slice_calls(env, op, dtype):
     ct, batched = env
     opts = _slices()
-    rb = batched.RaggedBatch(opts)
+    rb = batched.RaggedBatch(opts, dtype=dtype)
     g = torch.Generator().manual_seed(5)
     ins = []
     for o in opts:
         V, D, W, H = (int(o[i]) for i in range(4))
         shape = (1, 1, H, W) if op in ("projection", "backprojection_t") else (1, 1, V, D)
-        ins.append(torch.randn(shape, generator=g).cuda())
+        ins.append(torch.randn(shape, generator=g, dtype=torch.float64).to(dtype).cuda())
     got = rb.run(op, ins)
     for x, o, y in zip(ins, opts, got):
-        want = getattr(ct, op)(x, torch.tensor(o, dtype=torch.float32))
+        want = getattr(ct, op)(x, torch.tensor(o, dtype=dtype))
+        assert y.dtype == dtype
         assert torch.equal(y, want), (op, o, float((y - want).abs().max()))
+
+
+def test_ragged_rejects_mixed_dtypes(env):
+    ct, batched = env
+    from ctlib_gb300 import _native as N
+    import ctypes
+    opts = _slices()[:2]
+    p32 = ct.get_plan(torch.tensor(opts[0]), torch.float32, torch.device("cuda", 0))
+    p64 = ct.get_plan(torch.tensor(opts[1]), torch.float64, torch.device("cuda", 0))
+    arr = (ctypes.c_void_p * 2)(p32.handle.value, p64.handle.value)
+    h = ctypes.c_void_p()
+    assert N.lib().ctgb_ragged_create(ctypes.byref(h), arr, 2, 0) == N.ERR_INVALID
+    assert "dtype" in N.last_error()
 
 
 @pytest.mark.parametrize("branches", [0, 1, 3])
