@@ -4,17 +4,19 @@
     sinos = rb.projection([img_0, img_1, ...])          # list of 1 x 1 x V_i x D_i
     recs = rb.fbp(sinos)                                 # list of 1 x 1 x H_i x W_i
 
-Every stage of an operator is a single persistent launch over all slices
+Every stage of an operator is a single launch over all slices
 (``ctgb_ragged_run``): the task list is built once, longest tasks first, and
-per-slice pointers are kernel parameters, so a run can be captured in a CUDA
-graph: ``rb.graphed(op, inputs)`` returns a replayable callable over static
-input/output buffers.
+per-slice pointers and plans are kernel parameters, so a run can be captured in
+a CUDA graph: ``rb.graphed(op, inputs)`` returns a replayable callable over
+static input/output buffers.
 
-``rb.graphed(op, inputs, branches=k)`` (the default, k = 4) instead captures
-each slice's own per-slice launches (the staged image gather included) on k
+``rb.graphed(op, inputs, branches=k)`` with k > 0 instead captures each
+slice's own per-slice launches (the staged image gather included) on k
 parallel branches of the graph, slices assigned longest first to the least
 loaded branch: no launch or plan overhead per call, and small slices overlap
-one another. ``branches=0`` captures the persistent launches.
+one another. ``branches=0`` captures the one-launch-per-stage form, and the
+default ``branches="auto"`` the form the autotuner measured fastest for this
+batch (``tune.tune_ragged``, cached per batch signature).
 """
 
 from __future__ import annotations
@@ -104,17 +106,23 @@ class RaggedBatch:
     def fbp(self, sinos):
         return self.run(N.OP_FBP, sinos)
 
-    def graphed(self, ops, inputs, branches: int = 4):
+    def graphed(self, ops, inputs, branches="auto"):
         """Capture `ops` (one op name or a chain such as ("projection", "fbp"),
         each op consuming the previous one's outputs) into a CUDA graph over
         static copies of `inputs`. Returns (replay, static_inputs, outputs):
         copy new data into static_inputs, call replay(), read outputs.
-        branches = k > 0 (default 4): the slices' own launches on k parallel
-        graph branches; branches = 0: the persistent ragged launches."""
+        branches = k > 0: the slices' own launches on k parallel graph
+        branches; branches = 0: one launch per stage over all slices;
+        "auto" (default): the form the autotuner picked for this batch and
+        chain (tune.tune_ragged), timing the forms first if none is cached."""
         if isinstance(ops, str):
             ops = (ops,)
-        if branches < 0:
-            raise ValueError("branches must be >= 0")
+        if branches == "auto":
+            branches = tune.ragged_cached(self, ops)
+            if branches is None:
+                branches = tune.tune_ragged(self, ops, inputs)["branches"]
+        if not isinstance(branches, int) or branches < 0:
+            raise ValueError("branches must be 'auto' or an int >= 0")
         static_in = [x.clone() for x in inputs]
         if branches:
             return self._graphed_branches(ops, static_in, branches)

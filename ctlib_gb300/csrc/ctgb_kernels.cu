@@ -809,14 +809,12 @@ __host__ __device__ __forceinline__ int view_split(int views) { return views < 2
 // along a line the edges grow with k, and across lines each edge moves
 // monotonically because the source lies outside the image), and when it fits
 // the slot's window of cells it copies the cell records, the q planes of those
-// cells and the tile's line maps into a ring of kSlots shared-memory slots with TMA bulk
+// cells and the tile's line maps into a ring of kSlots<T, SB> shared-memory slots with TMA bulk
 // copies. Consumers then read only shared memory; a view whose footprint does
 // not fit is read from the global tables instead (same arithmetic, same
 // result). The window carries a margin of two cells on each side, so every cell
 // a pixel can reach (including the seed correction and the step back when the
 // offset is negative) lies inside it.
-constexpr int kSlots = 7;  // views in flight per CTA
-
 // pixel rows per consumer thread of the staged image gather: 2 up to 8 slices
 // per thread, where the per-view costs are shared by few slices (A^T of one
 // 512^2 slice, 1152 views: 2.10 to 1.65 ms, 4 rows 1.90 ms; of 8 slices: 2.25
@@ -835,6 +833,19 @@ struct PixSlot {
   static constexpr int kLpBytes = 32 * 4 * (int)sizeof(T);      // up to 32 line maps
   static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
 };
+
+// Views in flight per CTA: as many slots as fit beside the Kahan sums of 8 row
+// warps with three CTAs per SM (74 KB of dynamic shared memory each, leaving
+// room for the static arrays and the per-CTA reserve), at most 16. The ring
+// has to cover the time from a slot's release by the slowest row warp to its
+// refill landing; the few-slice slots are small, so those rings get deep (16
+// slots for one to four slices per thread, 11 for eight, 7 for sixteen).
+template <class T, int SB>
+constexpr int kSlots = [] {
+  constexpr int acc = 2 * kPixRows<SB> * SB * 256 * (int)sizeof(T);
+  constexpr int n = (74 * 1024 - acc - 1024) / PixSlot<T, SB>::kBytes;
+  return n > 16 ? 16 : (n < 4 ? 4 : n);
+}();
 
 // SV: single-view backprojection (src/fan_ed_kernel.cu:946-1161): each view's
 // sum goes to its own image, img[slice][view][row][col], with no sum over views.
@@ -855,6 +866,7 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
   constexpr int kWin = S::kWin;
+  constexpr int kSlots = ctgb::kSlots<T, SB>;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
   __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
   // slot header, two 16-byte words: (window start or -1, flags, first line,
@@ -1550,7 +1562,7 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   constexpr int PX = kPixRows<SB>;
   dim3 grid((g.W + 31) / 32, (g.H + wpc * PX - 1) / (wpc * PX), G);
   const int nt = 32 * (wpc + 1);
-  const size_t smem = (size_t)2 * PX * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots * PixSlot<T, SB>::kBytes;
+  const size_t smem = (size_t)2 * PX * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots<T, SB> * PixSlot<T, SB>::kBytes;
   auto launch = [&](auto kern, T mul, T div) -> int {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
@@ -2070,7 +2082,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
                         (const void*)k_rag_sino_rows<T, true>, nullptr, (const void*)k_rag_ramp<T>,
                         (const void*)k_rag_combine<T>};
   constexpr int kPX = kPixRows<1>;
-  r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots * PixSlot<T, 1>::kBytes;
+  r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots<T, 1> * PixSlot<T, 1>::kBytes;
   for (const void* f : {(const void*)k_rag_pix_gather<T, kAt>, (const void*)k_rag_pix_gather<T, kB>})
     CTGB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->pix_smem));
   const size_t ramp_smem = (size_t)5 * r->maxD * es;

@@ -15,6 +15,12 @@ kept, in memory and in a JSON cache on disk
 
 ``ops`` applies a cached schedule automatically; ``tune()`` measures (set
 ``CTLIB_GB300_AUTOTUNE=1`` to tune every new (plan, op, batch) on first use).
+
+Ragged batches have a schedule of their own, the form of their CUDA graph:
+one launch per stage over the task list of all slices (``branches=0``), or the
+slices' own launches spread over k parallel graph branches. ``tune_ragged``
+times each form on the batch's own inputs and caches the fastest under the
+batch's signature (every slice's options, the dtype, the operator chain).
 """
 
 from __future__ import annotations
@@ -134,3 +140,48 @@ def tune(plan, op: int, batch: int, reps: int = 3, candidates=None) -> dict:
     return {"slices_per_thread": sb, "warps_per_cta": warps, "unroll": unroll, "ms": best_ms,
             "candidates": [{"slices_per_thread": s, "warps_per_cta": w, "unroll": u, "ms": m}
                            for m, s, w, u in results]}
+
+
+RAGGED_CANDIDATES = (0, 1, 2, 4, 8)
+
+
+def _ragged_key(rb, ops) -> str:
+    import hashlib
+    name = torch.cuda.get_device_name(rb.device)
+    sig = repr((tuple(tuple(p.values) for p in rb.plans), str(rb.dtype), tuple(ops)))
+    return f"ragged|{name}|{hashlib.sha1(sig.encode()).hexdigest()}"
+
+
+def ragged_cached(rb, ops):
+    """The cached graph form (branch count, 0 = one launch per stage) of a
+    ragged batch's operator chain, or None."""
+    with _lock:
+        hit = _load().get(_ragged_key(rb, ops))
+    return None if hit is None else int(hit[0])
+
+
+def tune_ragged(rb, ops, inputs, reps: int = 3, candidates=RAGGED_CANDIDATES) -> dict:
+    """Time the graph forms of `ops` (a chain such as ("projection", "fbp")) on
+    the ragged batch `rb` with `inputs`, keep the fastest (CUDA events around
+    each replay, mean of `reps` after one warm-up replay)."""
+    if isinstance(ops, str):
+        ops = (ops,)
+    stream = torch.cuda.current_stream(rb.device)
+    results = []
+    for br in candidates:
+        replay, _, _ = rb.graphed(ops, inputs, branches=br)
+        replay()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            replay()
+        b.record(stream)
+        torch.cuda.synchronize(rb.device)
+        results.append((a.elapsed_time(b) / reps, br))
+        del replay
+    results.sort()
+    best_ms, best = results[0]
+    with _lock:
+        _load()[_ragged_key(rb, ops)] = [best, best_ms]
+        _save()
+    return {"branches": best, "ms": best_ms, "candidates": [{"branches": br, "ms": ms} for ms, br in results]}

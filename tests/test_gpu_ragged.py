@@ -116,3 +116,30 @@ def test_ragged_graph_outlives_batch(env, branches):
     for x, o, y in zip(imgs, opts, outs):
         ot = torch.tensor(o, dtype=torch.float32)
         assert torch.equal(y, ct.fbp(ct.projection(x, ot), ot))
+
+
+def test_ragged_autotuned_form(env, tmp_path, monkeypatch):
+    """tune.tune_ragged times every graph form, caches the fastest under the
+    batch's signature, and graphed(branches="auto") replays that form with the
+    per-slice results."""
+    ct, batched = env
+    from ctlib_gb300 import tune
+    monkeypatch.setenv("CTLIB_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(tune, "_cache", None)
+    opts = _slices()
+    rb = batched.RaggedBatch(opts)
+    from ctlib_gb300.workloads import ellipse_phantom
+    imgs = [torch.from_numpy(ellipse_phantom(int(o[3]), int(o[2]), o[4], 60 + i)[None, None]).cuda()
+            for i, o in enumerate(opts)]
+    chain = ("projection", "fbp")
+    assert tune.ragged_cached(rb, chain) is None
+    res = tune.tune_ragged(rb, chain, imgs, reps=1)
+    assert res["branches"] in tune.RAGGED_CANDIDATES
+    assert len(res["candidates"]) == len(tune.RAGGED_CANDIDATES)
+    assert tune.ragged_cached(rb, chain) == res["branches"]
+    replay, static_in, outs = rb.graphed(chain, imgs)
+    replay()
+    torch.cuda.synchronize()
+    for x, o, y in zip(imgs, opts, outs):
+        ot = torch.tensor(o, dtype=torch.float32)
+        assert torch.equal(y, ct.fbp(ct.projection(x, ot), ot))
