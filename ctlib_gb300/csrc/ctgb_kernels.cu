@@ -1450,9 +1450,10 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es) + pix_parts_bytes(g, op, batch, es);
 }
 
-// two straight-line steps are instantiated for the widths that carry batches
+// two straight-line steps are instantiated for every fp32 width (the autotuner
+// picks them per operator and batch; fp64 keeps three)
 template <class T, int SB>
-constexpr bool kTwoStep = sizeof(T) == 4 && SB >= 4;
+constexpr bool kTwoStep = sizeof(T) == 4;
 
 // plain-summation variants (no Kahan folds) are instantiated for fp32 with three
 // straight-line steps only: they serve error studies, not speed; for fp64 the

@@ -72,8 +72,8 @@ int ctgb_plan_set_schedule(ctgb_plan* plan, int op, int slices_per_thread, int w
  * the overlapped pixels per detector cell (projection, backprojection_t) or
  * cells per pixel (projection_t, backprojection, fbp) evaluated without a
  * branch before a remainder loop takes any further ones. 2 pays when few cells
- * (pixels) span three pixels (cells); fp32 with 4 or more slices per thread
- * only, other widths always use 3. Results do not depend on it. No counterpart
+ * (pixels) span three pixels (cells); fp32 only, fp64 always uses 3.
+ * Results do not depend on it. No counterpart
  * in the reference (its merge walk has no fixed step count). */
 int ctgb_plan_set_unroll(ctgb_plan* plan, int op, int steps);
 
