@@ -79,7 +79,7 @@ struct DevPlan {
   unsigned long long wait_ns;  // limit of each bounded wait in the staged image gather
   T dImg, s2r, dAng, wscale;
   const int* flags;   // V
-  const T* src;       // V*2   source x, y
+  const T* wsrc;      // V*2   weight source: equal-distance fans (sx, sy) / s2r^2, equal-angle (sx, sy)
   const T* db2;       // V*(D+1)*2  cell boundaries (hi, lo)
   const T* rec;       // V*Dp*4 cell records (db hi, db lo, width, next db hi); zero past D
   const T* wd;        // V*D   cell widths
@@ -323,11 +323,14 @@ __global__ void k_layout_sino(const T* __restrict__ y, T* __restrict__ q, const 
 // product: left to the compiler, which product it fuses can differ between
 // inlined copies, and every copy (staged or global view, one or more pixels per
 // thread, any schedule) must give the same weight bit for bit.
-// U^2 weight (src/fan_ed_kernel.cu:18-21)
+// U^2 weight (src/fan_ed_kernel.cu:18-21): r^2 / (r - d)^2, d = (sx x + sy y) / r
+// the pixel's distance along the source direction. Written 1 / t^2 with
+// t = 1 - (sx / r^2) x - (sy / r^2) y, where (nx, ny) = (sx, sy) / r^2 comes per
+// view from the plan (wsrc, formed in fp64), so that one division is left for
+// the caller to fold with its other divisors.
 template <class T>
-__device__ __forceinline__ T cweight_ed(T sx, T sy, T x, T y, T r) {
-  const T d = fma(sx, x, mul_rn(sy, y)) / r;
-  return r * r / ((r - d) * (r - d));
+__device__ __forceinline__ T ued_base(T nx, T ny, T x, T y) {
+  return T(1) - fma(nx, x, mul_rn(ny, y));
 }
 // squared source distance (src/fan_ea_kernel.cu:18-20), used as a divisor
 template <class T>
@@ -374,7 +377,7 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
   const T* lgv = P.lg + (size_t)v * P.L * 4;
   const T* lsv = P.ls + (size_t)v * P.L;
   T sx = T(0), sy = T(0);
-  if (KIND == kBt && P.scan != kPara) { sx = P.src[2 * v]; sy = P.src[2 * v + 1]; }
+  if (KIND == kBt && P.scan != kPara) { sx = P.wsrc[2 * v]; sy = P.wsrc[2 * v + 1]; }
   const T pc0 = xb ? P.colc[0] : P.rowc[P.H - 1];  // centre of pixel k = 0 along the walk
 
   extern __shared__ unsigned char det_smem[];
@@ -425,7 +428,8 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
         w *= sig;
       } else if (P.scan == kFanED) {
         const T pc = fma(T(kk), P.dImg, pc0);
-        w *= xb ? cweight_ed(sx, sy, pc, lc, P.s2r) : cweight_ed(sx, sy, lc, pc, P.s2r);
+        const T t = xb ? ued_base(sx, sy, pc, lc) : ued_base(sx, sy, lc, pc);
+        w /= t * t;
       } else if (P.scan == kFanEA) {
         const T pc = fma(T(kk), P.dImg, pc0);
         w /= xb ? dist2_ea(sx, sy, pc, lc) : dist2_ea(sx, sy, lc, pc);
@@ -712,7 +716,10 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
   // 1 / dImg), folded into each cell's overlap weight
   T wv = T(1);
   if (KIND == kB) {
-    if (P.scan == kFanED) wv = cweight_ed(sx, sy, pcx, pcy, P.s2r) / sig;
+    if (P.scan == kFanED) {
+      const T t = ued_base(sx, sy, pcx, pcy);
+      wv = T(1) / (t * t * sig);
+    }
     else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(sx, sy, pcx, pcy) * sig);
     else wv = T(1) / P.dImg;
   }
@@ -785,7 +792,7 @@ __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int 
   const bool xb = P.flags[v] & 1;
   const int k = xb ? c : P.H - 1 - r;
   const Quad<T> A4 = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r : c)) * 4);
-  pix_view<T, SB, KIND, U, false>(P, A4, T(k), load_seed(P.inv + (size_t)v * 5), P.src[2 * v], P.src[2 * v + 1], pcx,
+  pix_view<T, SB, KIND, U, false>(P, A4, T(k), load_seed(P.inv + (size_t)v * 5), P.wsrc[2 * v], P.wsrc[2 * v + 1], pcx,
                                   pcy, P.rec + (size_t)v * P.Dp * 4, qv, qs, 0, 0, P.D, blk);
 }
 
@@ -913,8 +920,8 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
       if (v >= vend) return;
       in.fl = P.flags[v];
       in.sd = load_seed(P.inv + (size_t)v * 5);
-      in.sx = P.src[2 * v];
-      in.sy = P.src[2 * v + 1];
+      in.sx = P.wsrc[2 * v];
+      in.sy = P.wsrc[2 * v + 1];
       const bool xb = in.fl & 1;
       in.A4[0] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r0 : c0)) * 4);
       in.A4[1] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r1 : c1)) * 4);
@@ -1375,7 +1382,12 @@ static int upload(ctgb_plan* p) {
   }
   for (int r = 0; r < g.H; ++r) rowc[r] = (g.height / 2 - r - 0.5) * g.dImg;
   for (int c = 0; c < g.W; ++c) colc[c] = (c - g.width / 2 + 0.5) * g.dImg;
-  const std::vector<const std::vector<double>*> tabs = {&g.src, &db2, &g.wd, &g.fq, &g.fbt, &lg, &ls, &lp,
+  // the backprojector weights' source table: equal-distance fans need the source
+  // position only divided by s2r^2 (ued_base), formed here in fp64
+  std::vector<double> wsrc = g.src;
+  if (g.scan == kFanED)
+    for (double& x : wsrc) x /= (double)g.s2r * (double)g.s2r;
+  const std::vector<const std::vector<double>*> tabs = {&wsrc, &db2, &g.wd, &g.fq, &g.fbt, &lg, &ls, &lp,
                                                         &rowc, &colc, &g.wpre, &g.taps, &g.taps_lo, &rec};
   size_t off = 0;
   std::vector<size_t> offs;
@@ -1398,7 +1410,7 @@ static int upload(ctgb_plan* p) {
   DevPlan<T> P{};
   P.V = V; P.D = D; P.W = g.W; P.H = g.H; P.L = L; P.scan = g.scan;
   P.dImg = (T)g.dImg; P.s2r = (T)g.s2r; P.dAng = (T)g.dAng; P.wscale = (T)g.wscale;
-  P.src = reinterpret_cast<const T*>(b + offs[0]);
+  P.wsrc = reinterpret_cast<const T*>(b + offs[0]);
   P.db2 = reinterpret_cast<const T*>(b + offs[1]);
   P.wd = reinterpret_cast<const T*>(b + offs[2]);
   P.fq = reinterpret_cast<const T*>(b + offs[3]);
@@ -1826,7 +1838,8 @@ __global__ void __launch_bounds__(256) k_rag_sino_rows(const DevPlan<T>* __restr
 }
 
 // The staged image gather of k_pix_gather (one slice per thread, two pixel
-// rows, three straight-line cells), each CTA one task of the task list: the
+// rows, two straight-line cells in fp32, three in fp64; the step count never
+// changes results), each CTA one task of the task list: the
 // same arithmetic, view parts and fold points as a per-slice call, so the
 // results are the same bit for bit. Sinogram planes [V][Dp] per slice at
 // off_q, partial images [parts][H][W] at off_parts.
@@ -1837,7 +1850,7 @@ __global__ void __launch_bounds__(32 * (kRagPixWarps + 1), 3)
                      const size_t* __restrict__ off_parts, int fbp_scale) {
   const RPixTask t = tasks[blockIdx.x];
   const DevPlan<T>& P = rp.p[t.slice];
-  pix_gather_cta<T, 1, KIND, 3, false, kPixRows<1>, false>(
+  pix_gather_cta<T, 1, KIND, kTwoStep<T, 1> ? 2 : 3, false, kPixRows<1>, false>(
       P, reinterpret_cast<const T*>(ws + off_q[t.slice]), io.out[t.slice],
       reinterpret_cast<T*>(ws + off_parts[t.slice]), 1, fbp_scale ? P.dAng : T(1), fbp_scale ? T(2) : T(1),
       view_split(P.V), t.bx, t.by, t.part);
