@@ -1777,13 +1777,14 @@ constexpr int kRagPixWarps = 8;
 constexpr int kRagPixRows = kRagPixWarps * kPixRows<1>;
 
 template <class T>
-__global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<T>* __restrict__ plans,
-                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
-                                                       unsigned char* ws, const size_t* __restrict__ off) {
+__global__ void __launch_bounds__(256) k_rag_transpose(const __grid_constant__ RaggedPlans<T> rp,
+                                                       const RTask* __restrict__ tasks, int ntasks,
+                                                       const __grid_constant__ RaggedIO<T> io, unsigned char* ws,
+                                                       const size_t* __restrict__ off) {
   __shared__ T tile[32][33];
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const int H = plans[tk.slice].H, W = plans[tk.slice].W;
+    const int H = rp.p[tk.slice].H, W = rp.p[tk.slice].W;
     const T* img = io.in[tk.slice];
     T* imy = reinterpret_cast<T*>(ws + off[tk.slice]);
     const int r0 = tk.a * 32, c0 = tk.b * 32;
@@ -1800,28 +1801,35 @@ __global__ void __launch_bounds__(256) k_rag_transpose(const DevPlan<T>* __restr
   }
 }
 
+// The detector gather of a per-slice call with one slice per thread (two
+// straight-line pixels in fp32, three in fp64; the step count never changes
+// results), each CTA walking the task list; the slice's plan is read in place
+// from the constant bank.
 template <class T, int KIND>
-__global__ void __launch_bounds__(256) k_rag_det_gather(const DevPlan<T>* __restrict__ plans,
-                                                        const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
-                                                        unsigned char* ws, const size_t* __restrict__ off) {
+__global__ void __launch_bounds__(256) k_rag_det_gather(const __grid_constant__ RaggedPlans<T> rp,
+                                                        const RTask* __restrict__ tasks, int ntasks,
+                                                        const __grid_constant__ RaggedIO<T> io, unsigned char* ws,
+                                                        const size_t* __restrict__ off) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<T> P = plans[tk.slice];
+    const DevPlan<T>& P = rp.p[tk.slice];
     const int v = tk.a * (blockDim.x >> 5) + warp, d = tk.b * 32 + lane;
     if (v < P.V && d < P.D)
-      det_gather_cell<T, 1, KIND, 3>(P, v, d, 0, io.in[tk.slice], reinterpret_cast<const T*>(ws + off[tk.slice]),
-                                     (size_t)P.W, (size_t)P.H, io.out[tk.slice], 1);
+      det_gather_cell<T, 1, KIND, kTwoStep<T, 1> ? 2 : 3>(P, v, d, 0, io.in[tk.slice],
+                                                          reinterpret_cast<const T*>(ws + off[tk.slice]),
+                                                          (size_t)P.W, (size_t)P.H, io.out[tk.slice], 1);
   }
 }
 
 template <class T, bool SCALE>
-__global__ void __launch_bounds__(256) k_rag_sino_rows(const DevPlan<T>* __restrict__ plans,
-                                                       const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
-                                                       unsigned char* ws, const size_t* __restrict__ off) {
+__global__ void __launch_bounds__(256) k_rag_sino_rows(const __grid_constant__ RaggedPlans<T> rp,
+                                                       const RTask* __restrict__ tasks, int ntasks,
+                                                       const __grid_constant__ RaggedIO<T> io, unsigned char* ws,
+                                                       const size_t* __restrict__ off) {
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<T> P = plans[tk.slice];
+    const DevPlan<T>& P = rp.p[tk.slice];
     const int v = tk.a, D = P.D;
     const bool flip = P.flags[v] & 2;
     const T* y = io.in[tk.slice] + (size_t)v * D;
@@ -1880,13 +1888,14 @@ __global__ void __launch_bounds__(256) k_rag_combine(const __grid_constant__ Rag
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_rag_ramp(const DevPlan<T>* __restrict__ plans,
-                                                  const RTask* __restrict__ tasks, int ntasks, RaggedIO<T> io,
-                                                  unsigned char* ws, const size_t* __restrict__ off) {
+__global__ void __launch_bounds__(256) k_rag_ramp(const __grid_constant__ RaggedPlans<T> rp,
+                                                  const RTask* __restrict__ tasks, int ntasks,
+                                                  const __grid_constant__ RaggedIO<T> io, unsigned char* ws,
+                                                  const size_t* __restrict__ off) {
   extern __shared__ unsigned char smem_raw[];
   for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
     const RTask tk = tasks[t];
-    const DevPlan<T> P = plans[tk.slice];
+    const DevPlan<T>& P = rp.p[tk.slice];
     ramp_filter_view<T, 1>(P, tk.a, 0, io.in[tk.slice], reinterpret_cast<T*>(ws + off[tk.slice]), P.Dp, 1,
                            reinterpret_cast<T*>(smem_raw));
   }
@@ -1987,8 +1996,7 @@ struct RaggedStage {
 struct ctgb_ragged {
   int n = 0, device = 0, maxD = 0, dtype = 0;
   void* dev = nullptr;
-  const void* plans = nullptr;  // device copy (DevPlan<T>[n]), for the kernels that walk a task list
-  void* host_plans = nullptr;   // the same plans (RaggedPlans<T>), passed by value to the image gather
+  void* host_plans = nullptr;  // every slice's DevPlan<T> (RaggedPlans<T>), passed by value to the kernels
   const size_t* off_img = nullptr;    // per slice: transposed image in the workspace
   const size_t* off_sino = nullptr;   // per slice: sinogram planes [V][Dp] in the workspace
   const size_t* off_parts = nullptr;  // per slice: partial images of the view parts
@@ -2058,7 +2066,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   auto by_len = [](const auto& x, const auto& y) { return x.first > y.first; };
   for (auto* v : {&tr, &dg, &rw, &rp, &cb}) std::stable_sort(v->begin(), v->end(), by_len);
   std::stable_sort(pg.begin(), pg.end(), by_len);
-  const size_t b_plans = al(sizeof(DevPlan<T>) * n), b_off = al(sizeof(size_t) * n);
+  const size_t b_off = al(sizeof(size_t) * n);
   std::vector<std::pair<std::vector<unsigned char>, size_t>> lists;  // bytes, entries
   auto pack = [&](const auto& v) {
     using E = typename std::decay_t<decltype(v)>::value_type::second_type;
@@ -2067,7 +2075,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     lists.push_back({std::move(b), v.size()});
   };
   pack(tr); pack(dg); pack(rw); pack(pg); pack(rp); pack(cb);
-  size_t total = b_plans + 3 * b_off;
+  size_t total = 3 * b_off;
   for (auto& l : lists) total += al(l.first.size() ? l.first.size() : 1);
   std::vector<unsigned char> host(total, 0);
   size_t o = 0;
@@ -2077,7 +2085,6 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     o += span;
     return at;
   };
-  const size_t o_plans = put(dp.data(), sizeof(DevPlan<T>) * n, b_plans);
   const size_t o_oi = put(oi.data(), sizeof(size_t) * n, b_off);
   const size_t o_os = put(os.data(), sizeof(size_t) * n, b_off);
   const size_t o_op = put(opt.data(), sizeof(size_t) * n, b_off);
@@ -2087,7 +2094,6 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   CTGB_CUDA(cudaMalloc(&r->dev, total));
   CTGB_CUDA(cudaMemcpy(r->dev, host.data(), total, cudaMemcpyHostToDevice));
   unsigned char* base = static_cast<unsigned char*>(r->dev);
-  r->plans = base + o_plans;
   r->off_img = reinterpret_cast<const size_t*>(base + o_oi);
   r->off_sino = reinterpret_cast<const size_t*>(base + o_os);
   r->off_parts = reinterpret_cast<const size_t*>(base + o_op);
@@ -2128,29 +2134,28 @@ static int ragged_run_t(const ctgb_ragged* r, int op, const void* const* in, voi
     io.in[i] = static_cast<const T*>(in[i]);
     io.out[i] = static_cast<T*>(out[i]);
   }
-  const DevPlan<T>* plans = static_cast<const DevPlan<T>*>(r->plans);
   const RaggedPlans<T>& hp = *static_cast<const RaggedPlans<T>*>(r->host_plans);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned char* w = static_cast<unsigned char*>(ws);
   auto rt = [](const RaggedStage& s) { return static_cast<const RTask*>(s.tasks); };
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
-    k_rag_transpose<T><<<r->transpose.grid, 256, 0, st>>>(plans, rt(r->transpose), r->transpose.n, io, w,
+    k_rag_transpose<T><<<r->transpose.grid, 256, 0, st>>>(hp, rt(r->transpose), r->transpose.n, io, w,
                                                           r->off_img);
     const size_t acc_smem = (size_t)2 * 256 * sizeof(T);
     if (op == CTGB_OP_PROJECTION)
-      k_rag_det_gather<T, kA><<<r->detg.grid, 256, acc_smem, st>>>(plans, rt(r->detg), r->detg.n, io, w,
+      k_rag_det_gather<T, kA><<<r->detg.grid, 256, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
                                                                    r->off_img);
     else
-      k_rag_det_gather<T, kBt><<<r->detg.grid, 256, acc_smem, st>>>(plans, rt(r->detg), r->detg.n, io, w,
+      k_rag_det_gather<T, kBt><<<r->detg.grid, 256, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
                                                                     r->off_img);
   } else {
     if (op == CTGB_OP_FBP) {
       const size_t smem = (size_t)5 * r->maxD * sizeof(T);
-      k_rag_ramp<T><<<r->ramp.grid, 256, smem, st>>>(plans, rt(r->ramp), r->ramp.n, io, w, r->off_sino);
+      k_rag_ramp<T><<<r->ramp.grid, 256, smem, st>>>(hp, rt(r->ramp), r->ramp.n, io, w, r->off_sino);
     } else if (op == CTGB_OP_PROJECTION_T) {
-      k_rag_sino_rows<T, true><<<r->rows.grid, 256, 0, st>>>(plans, rt(r->rows), r->rows.n, io, w, r->off_sino);
+      k_rag_sino_rows<T, true><<<r->rows.grid, 256, 0, st>>>(hp, rt(r->rows), r->rows.n, io, w, r->off_sino);
     } else {
-      k_rag_sino_rows<T, false><<<r->rows.grid, 256, 0, st>>>(plans, rt(r->rows), r->rows.n, io, w, r->off_sino);
+      k_rag_sino_rows<T, false><<<r->rows.grid, 256, 0, st>>>(hp, rt(r->rows), r->rows.n, io, w, r->off_sino);
     }
     const RPixTask* pt = static_cast<const RPixTask*>(r->pixg.tasks);
     const int nt = 32 * (kRagPixWarps + 1);
