@@ -568,6 +568,12 @@ def run_ours(args):
         parity = {"projection_rel_l2_vs_fp64": oracle.rel_l2(a_got, a_ref),
                   "projection_t_rel_l2_vs_fp64": oracle.rel_l2(at_got, at_ref)}
 
+    # kernels of this package per timed step: image layout + detector gather,
+    # sinogram layout + image gather, and the sum of the image gather's view
+    # parts when it splits the views (V / 128 parts up to 8, one below 256 views:
+    # view_split in csrc/ctgb_kernels.cu)
+    launches_per_step = 4 + (1 if V >= 256 else 0)
+
     # -- roofline of the dominant kernel -------------------------------------
     ta, tat = statistics.mean(t_a), statistics.mean(t_at)
     ka, kat = _kernel_times(plan, args.steps, flush, stream, lambda: ctlib.projection(img, opts),
@@ -625,7 +631,7 @@ def run_ours(args):
                                   "note": "A^T(Ax - y) for the same batch: ctgb_data_gradient vs projection, "
                                           "subtraction, projection_t"},
                 "laplacian": lap,
-                "gpu_launches": 4 * args.steps,
+                "gpu_launches": args.steps * launches_per_step,
                 "clocks": clocks, "roofline": roof, "roofline_fp32": roof_fp32, "parity": parity,
                 "cpu_baseline": cb}
         print(json.dumps(line), flush=True)

@@ -2020,8 +2020,6 @@ static void free_host_plans(ctgb_ragged* r) {
 
 template <class T>
 static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
-  int sms = 0;
-  CTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r->device));
   std::vector<DevPlan<T>> dp(n);
   std::vector<size_t> oi(n), os(n), opt(n);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -2098,9 +2096,6 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   r->off_sino = reinterpret_cast<const size_t*>(base + o_os);
   r->off_parts = reinterpret_cast<const size_t*>(base + o_op);
   RaggedStage* st[6] = {&r->transpose, &r->detg, &r->rows, &r->pixg, &r->ramp, &r->combine};
-  const void* fns[6] = {(const void*)k_rag_transpose<T>, (const void*)k_rag_det_gather<T, kA>,
-                        (const void*)k_rag_sino_rows<T, true>, nullptr, (const void*)k_rag_ramp<T>,
-                        (const void*)k_rag_combine<T>};
   constexpr int kPX = kPixRows<1>;
   r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots<T, 1> * PixSlot<T, 1>::kBytes;
   for (const void* f : {(const void*)k_rag_pix_gather<T, kAt>, (const void*)k_rag_pix_gather<T, kB>})
@@ -2109,18 +2104,14 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   if (ramp_smem > 48 * 1024)
     CTGB_CUDA(cudaFuncSetAttribute((const void*)k_rag_ramp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)ramp_smem));
+  // one CTA per task in every stage: the block scheduler hands tasks out in
+  // list order (longest first) as CTAs finish, which balances the stage; a
+  // persistent grid walking the list with a fixed stride left some CTAs with
+  // far more work than others
   for (int i = 0; i < 6; ++i) {
     st[i]->tasks = base + o_stage[i];
     st[i]->n = (int)lists[i].second;
-    if (i == 3) {  // image gather: one CTA per task
-      st[i]->grid = st[i]->n;
-      continue;
-    }
-    int per_sm = 1;
-    const size_t smem = i == 4 ? ramp_smem : i == 1 ? (size_t)2 * 256 * es : 0;
-    CTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 256, smem));
-    const int cap = sms * (per_sm > 0 ? per_sm : 1);
-    st[i]->grid = st[i]->n < cap ? st[i]->n : cap;
+    st[i]->grid = st[i]->n;
   }
   return CTGB_OK;
 }
