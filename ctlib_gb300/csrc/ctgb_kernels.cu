@@ -1198,27 +1198,46 @@ __global__ void __launch_bounds__(256) k_combine_parts(const T* __restrict__ par
 // for one slice: outputs k0, k0+2, ..., k0+14 only meet taps of odd offset (the
 // even non-zero offsets of the RL kernel are zero), plus the centre tap.
 // ----------------------------------------------------------------------------
-// Called by every thread of the CTA; `smem` holds 4D + SB*D elements. In fp32
-// the taps are pairs (taps, tapl) and the low parts are summed separately.
+// Called by every thread of the CTA; `smem` holds ramp_smem_elems(D, SB)
+// elements. In fp32 the taps are pairs (taps, tapl) and the low parts are summed
+// separately.
+//
+// Shared-memory layout. A warp's threads produce outputs whose tap indices are
+// 16 apart, and its slices' input rows lie D apart; stored plainly, the taps
+// would be read 8 ways and, for D a multiple of 32, the rows 16 ways onto one
+// bank. Tap index t (padded by kTapPad zero taps on both sides, so no index the
+// loop forms needs a range check) sits at word t + t / 32, and the rows have an
+// odd stride D + 1: both then spread over the banks.
+constexpr int kTapPad = 32;
+__host__ __device__ __forceinline__ int tap_slot(int t) { return t + (t >> 5); }
+__host__ __device__ __forceinline__ size_t ramp_smem_elems(int D, int SB) {
+  const int ntap = 2 * D - 1 + 2 * kTapPad;  // padded tap indices 0 .. ntap-1
+  return 2 * (size_t)tap_slot(ntap) + (size_t)SB * (D + 1);
+}
+
 template <class T, int SB, bool PLAIN = false>
 __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int g, const T* __restrict__ y,
                                                  T* __restrict__ q, int qs, int B, T* smem) {
   constexpr bool kLo = sizeof(T) == 4;
   const int D = P.D;
-  T* taps = smem;              // 2D-1 (+1)
-  T* tapl = taps + 2 * D;      // 2D-1 (+1)
-  T* rows = tapl + 2 * D;      // SB x D
+  const int ntap = 2 * D - 1 + 2 * kTapPad;
+  T* taps = smem;                       // tap index t at taps[tap_slot(t + kTapPad)]
+  T* tapl = taps + tap_slot(ntap);      // the same for the low parts
+  T* rows = tapl + tap_slot(ntap);      // SB rows of stride D + 1
+  const int rs = D + 1;
   __syncthreads();  // smem may still be read by a previous task of this CTA
-  for (int j = threadIdx.x; j < 2 * D - 1; j += blockDim.x) {
-    taps[j] = P.taps[j];
-    tapl[j] = kLo ? P.tapl[j] : T(0);
+  for (int j = threadIdx.x; j < ntap; j += blockDim.x) {
+    const int t = j - kTapPad;
+    const bool in = t >= 0 && t < 2 * D - 1;
+    taps[tap_slot(j)] = in ? P.taps[t] : T(0);
+    tapl[tap_slot(j)] = (kLo && in) ? P.tapl[t] : T(0);
   }
   for (int i = threadIdx.x; i < SB * D; i += blockDim.x) {
     const int s = i / D, m = i % D;
     const int bb = g * SB + s;
     T val = T(0);
     if (bb < B) val = (y[((size_t)bb * P.V + v) * D + m] * P.wpre[m]) * P.wscale;
-    rows[s * D + m] = val;
+    rows[s * rs + m] = val;
   }
   __syncthreads();
   const int chunks = (D + 15) / 16;               // 16 outputs (8 per parity) per chunk
@@ -1233,7 +1252,7 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     const int par = (it / SB) & 1;
     const int ch = it / (2 * SB);
     const int k0 = ch * 16 + par;
-    const T* row = rows + s * D;
+    const T* row = rows + s * rs;
     // blocks of 16 taps are summed plainly (part) and folded into acc with
     // Kahan compensation (comp): the ramp filter cancels strongly, so the
     // far, small taps must not be added straight onto the large running sum;
@@ -1249,13 +1268,14 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     int step = 0;
     // one pass over the inputs m = m0, m0+2, ...: window win[i] = h(m - k0 - 2i)
     auto pass = [&](int m0) {
+      // tap indices run from -15 (first window of the last chunk, k0 <= D) to 2D (last new
+      // tap), inside the kTapPad zero margins
       T win[8], wlo[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const int ti = m0 - k0 - 2 * i + D - 1;
-        const bool ok = ti >= 0 && ti < 2 * D - 1;
-        win[i] = ok ? taps[ti] : T(0);
-        wlo[i] = ok ? tapl[ti] : T(0);
+        const int ts = tap_slot(m0 - k0 - 2 * i + D - 1 + kTapPad);
+        win[i] = taps[ts];
+        wlo[i] = tapl[ts];
       }
       for (int m = m0; m < D; m += 2, ++step) {
         const T xm = row[m];
@@ -1270,10 +1290,9 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
           win[i] = win[i - 1];
           wlo[i] = wlo[i - 1];
         }
-        const int ti = m + 2 - k0 + D - 1;
-        const bool ok = ti >= 0 && ti < 2 * D - 1;
-        win[0] = ok ? taps[ti] : T(0);
-        wlo[0] = ok ? tapl[ti] : T(0);
+        const int ts = tap_slot(m + 2 - k0 + D - 1 + kTapPad);
+        win[0] = taps[ts];
+        wlo[0] = tapl[ts];
         if (!PLAIN && (step & 15) == 15) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
@@ -1290,7 +1309,7 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
     if (P.even_taps) pass(par);   // windowed kernels: even offsets, the centre tap included
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[i] = add_rn(acc[i], sub_rn(part[i], comp[i]));
-    const T h0 = taps[D - 1], h0l = tapl[D - 1];
+    const T h0 = taps[tap_slot(D - 1 + kTapPad)], h0l = tapl[tap_slot(D - 1 + kTapPad)];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int k = k0 + 2 * i;
@@ -1552,13 +1571,18 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   const HostGeom& g = p->geom;
   const bool plain = kPlainBuilt<T> && p->plain && op != CTGB_OP_BACKPROJECTION_SV;
   if (!planes_ready && op == CTGB_OP_FBP) {
-    const size_t smem = ((size_t)4 * g.D + (size_t)SB * g.D) * sizeof(T);
+    const size_t smem = ramp_smem_elems(g.D, SB) * sizeof(T);
     auto ramp = plain ? k_ramp_filter<T, SB, kPlainBuilt<T>> : k_ramp_filter<T, SB>;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(ramp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("ramp filter smem: ") + cudaGetErrorString(e));
     }
-    ramp<<<dim3(g.V, G), 256, smem, st>>>(P, x, qb, batch);
+    // one thread per work item (8 outputs of one parity and slice) up to 256:
+    // a one-slice row of 736 bins is 92 items, which a 256-thread CTA would
+    // leave mostly idle
+    const int items = SB * 2 * ((g.D + 15) / 16);
+    const int nt = std::min(256, std::max(32, (items + 31) / 32 * 32));
+    ramp<<<dim3(g.V, G), nt, smem, st>>>(P, x, qb, batch);
   } else if (!planes_ready) {
     const int tb = 256;
     const int nb = (int)std::min<size_t>((size_t)G * g.V * Planes<SB>::NQ, 152 * 16);
@@ -2100,7 +2124,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots<T, 1> * PixSlot<T, 1>::kBytes;
   for (const void* f : {(const void*)k_rag_pix_gather<T, kAt>, (const void*)k_rag_pix_gather<T, kB>})
     CTGB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->pix_smem));
-  const size_t ramp_smem = (size_t)5 * r->maxD * es;
+  const size_t ramp_smem = ramp_smem_elems(r->maxD, 1) * es;
   if (ramp_smem > 48 * 1024)
     CTGB_CUDA(cudaFuncSetAttribute((const void*)k_rag_ramp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)ramp_smem));
@@ -2141,8 +2165,10 @@ static int ragged_run_t(const ctgb_ragged* r, int op, const void* const* in, voi
                                                                     r->off_img);
   } else {
     if (op == CTGB_OP_FBP) {
-      const size_t smem = (size_t)5 * r->maxD * sizeof(T);
-      k_rag_ramp<T><<<r->ramp.grid, 256, smem, st>>>(hp, rt(r->ramp), r->ramp.n, io, w, r->off_sino);
+      const size_t smem = ramp_smem_elems(r->maxD, 1) * sizeof(T);
+      // one slice per task: 2 * ceil(D / 16) work items, 46 to 128 for rows of
+      // 368 to 1024 bins
+      k_rag_ramp<T><<<r->ramp.grid, 128, smem, st>>>(hp, rt(r->ramp), r->ramp.n, io, w, r->off_sino);
     } else if (op == CTGB_OP_PROJECTION_T) {
       k_rag_sino_rows<T, true><<<r->rows.grid, 256, 0, st>>>(hp, rt(r->rows), r->rows.n, io, w, r->off_sino);
     } else {
