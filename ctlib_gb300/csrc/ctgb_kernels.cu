@@ -1277,7 +1277,48 @@ __device__ __forceinline__ void ramp_filter_view(const DevPlan<T>& P, int v, int
         win[i] = taps[ts];
         wlo[i] = tapl[ts];
       }
-      for (int m = m0; m < D; m += 2, ++step) {
+      int m = m0;
+      // blocks of 8 steps: at a block's start win[i] holds tap(base + m - 2i)
+      // (base = D - 1 - k0); the block loads nw[j] = tap(base + m + 2(j + 1)), and
+      // step t of the block gives output i the tap base + m + 2(t - i), which is
+      // win[i - t] for t <= i and nw[t - i - 1] otherwise: fixed registers, no
+      // window shifts. Same FMAs, same order and fold points as one step at a
+      // time below.
+      for (; m + 14 < D; m += 16, step += 8) {
+        T nw[8], nl[8], xv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int ts = tap_slot(m + 2 * (j + 1) - k0 + D - 1 + kTapPad);
+          nw[j] = taps[ts];
+          nl[j] = tapl[ts];
+          xv[j] = row[m + 2 * j];
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) part[i] = fma(xv[t], t <= i ? win[i - t] : nw[t - i - 1], part[i]);
+          if constexpr (kLo) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) plo[i] = fma(xv[t], t <= i ? wlo[i - t] : nl[t - i - 1], plo[i]);
+          }
+          if (!PLAIN && ((step + t) & 15) == 15) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              const T y = sub_rn(part[i], comp[i]);
+              const T tt = add_rn(acc[i], y);
+              comp[i] = sub_rn(sub_rn(tt, acc[i]), y);
+              acc[i] = tt;
+              part[i] = T(0);
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          win[i] = nw[7 - i];
+          wlo[i] = nl[7 - i];
+        }
+      }
+      for (; m < D; m += 2, ++step) {
         const T xm = row[m];
 #pragma unroll
         for (int i = 0; i < 8; ++i) part[i] = fma(xm, win[i], part[i]);
