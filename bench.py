@@ -596,7 +596,8 @@ def run_ours(args):
             "timing": "CUDA events recorded by the library right around the kernel, mean of the timed steps"}
     roof_fp32 = None
     if peak:
-        # survey model: 8 FP32 lane-ops per ray-update at the measured FFMA rate
+        # model: 8 FP32 lane-ops per ray-update (two overlap segments of min, max,
+        # subtract and FMA each) at the measured FFMA rate
         model_peak = peak["lane_ops_per_s"] / 8.0
         ru_dom = w.ray_updates()
         ach = ru_dom / (dom_ms / 1e3)
