@@ -34,6 +34,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -74,7 +75,7 @@ int fail(int code, const std::string& msg) {
 template <class T>
 struct DevPlan {
   int V, D, W, H, L, scan;
-  int Dp;             // D rounded up to a multiple of 4: row stride of cell records and sinogram planes
+  int Dp;             // padded_cells(D): row stride of cell records and sinogram planes
   int even_taps;      // fbp filter with non-zero even offsets (windowed kernels), besides the centre
   unsigned long long wait_ns;  // limit of each bounded wait in the staged image gather
   T dImg, s2r, dAng, wscale;
@@ -87,7 +88,7 @@ struct DevPlan {
   const T* fbt;       // V*D   EA B^T factor
   const T* lg;        // V*L*4 (1/sigma hi, 1/sigma lo, floor(beta), beta - floor(beta)), beta = -alpha/sigma
   const T* ls;        // V*L   sigma
-  const T* lp;        // V*L*4 (alpha hi, alpha lo, sigma hi, sigma lo)
+  const T* lp;        // V*L*4 (alpha hi, alpha lo, sigma hi, sigma lo), hi parts on a common grid
   const float* inv;   // V*5   cell-index seed
   const T* rowc;      // H: row centre y
   const T* colc;      // W: column centre x
@@ -95,6 +96,12 @@ struct DevPlan {
   const T* taps;      // 2D-1
   const T* tapl;      // 2D-1  fp64 taps minus taps (fp32 plans)
 };
+
+// Cells per row of the cell records and sinogram planes: D plus two padding
+// cells (zero width, zero samples), rounded up to a multiple of 4. The image
+// gather's straight-line steps read up to two cells past the pixel's first one
+// without a range check; past D they read a padding cell, whose overlap is 0.
+__host__ __device__ __forceinline__ int padded_cells(int D) { return (D + 2 + 3) & ~3; }
 
 template <class T>
 struct VecT;
@@ -498,7 +505,13 @@ __device__ __forceinline__ void det_gather_cell(const DevPlan<T>& P, int v, int 
         }
         vals[i] = mul_rn(r, fac);
       }
-      store_q<T, QW>(ro.q + ((((size_t)g * P.V + v) * NQ + qd) * P.Dp + d) * QW, vals);
+      T* qrow = ro.q + (((size_t)g * P.V + v) * NQ + qd) * P.Dp * QW;
+      store_q<T, QW>(qrow + (size_t)d * QW, vals);
+      if (d == P.D - 1) {  // the row's padding cells
+#pragma unroll
+        for (int i = 0; i < QW; ++i) vals[i] = T(0);
+        for (int dd = P.D; dd < P.Dp; ++dd) store_q<T, QW>(qrow + (size_t)dd * QW, vals);
+      }
     }
   } else {
 #pragma unroll
@@ -675,19 +688,17 @@ struct CellSpan {
 
 // Geometry of one view for one pixel (lower edge index k on its line, line
 // map A4): exact edge, seeded and corrected cell search, U straight-line
-// overlaps (cells past the pixel or the range get weight 0 on a clamped, valid
-// cell).
+// overlaps. Cells past the pixel get weight 0; the straight-line steps may run
+// up to U - 1 cells past dhi, onto the zero-width padding cells of the tables
+// (or of a staged window, which always holds them when it reaches D).
 template <class T, int KIND, int U, bool SM>
 __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, T kf, const Seed& sd, T sx, T sy,
                                          T pcx, T pcy, const T* __restrict__ rec, int base, int dlo, int dhi,
                                          CellSpan<T, U>& cs) {
-  // x = alpha + sigma*k as (xs, xl)
-  const T qh = mul_rn(A4.z, kf);
-  const T ql = fma(A4.z, kf, -qh);
-  const T xs = add_rn(A4.x, qh);
-  const T bv = sub_rn(xs, A4.x);
-  const T xe = add_rn(sub_rn(A4.x, sub_rn(xs, bv)), sub_rn(qh, bv));
-  const T xl = add_rn(xe, add_rn(A4.y, fma(A4.w, kf, ql)));
+  // x = alpha + sigma*k as (xs, xl): the line map's high parts lie on a grid
+  // that makes alpha_hi + sigma_hi*k exact for every edge of the line
+  const T xs = fma(A4.z, kf, A4.x);
+  const T xl = fma(A4.w, kf, A4.y);
   // seed the cell and correct it: db_hi[d] <= xs < db_hi[d+1], d in [dlo, dhi)
   int d = seed_cell(P.scan, (float)xs, sd, dlo, dhi);
   Quad<T> rd = ldrec<T, SM>(rec + (d - base) * 4);
@@ -725,11 +736,10 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
   }
 #pragma unroll
   for (int j = 0; j < U; ++j) {
-    const bool inside = d + j < dhi;
-    cs.oj[j] = (inside ? d + j : dhi - 1) - base;
+    cs.oj[j] = d + j - base;
     const T w = j == 0 ? w0 : rec[cs.oj[j] * 4 + 2];
     T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-    cs.ov[j] = (inside && ov > T(0)) ? (KIND == kB ? ov * wv : ov) : T(0);
+    cs.ov[j] = ov > T(0) ? (KIND == kB ? ov * wv : ov) : T(0);
     a -= w;
     b -= w;
   }
@@ -957,8 +967,9 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
         dmin = min(dmin, dd);
         dmax = max(dmax, dd);
       }
+      // two cells of margin, or up to the second padding cell past D
       const int lo = max(0, dmin - 2) & ~3;
-      const int hi = min(D - 1, dmax + 2);
+      const int hi = min(D + 1, dmax + 2);
       return hi < lo + kWin ? lo : -1;
     };
     ViewIn cur, nxt;
@@ -1419,7 +1430,7 @@ static int upload(ctgb_plan* p) {
     db2[2 * i] = hi;
     db2[2 * i + 1] = g.db[i] - hi;
   }
-  const int Dp = (D + 3) & ~3;
+  const int Dp = padded_cells(D);
   std::vector<double> rec((size_t)V * Dp * 4, 0.0);
   for (int v = 0; v < V; ++v)
     for (int d = 0; d < D; ++d) {
@@ -1437,7 +1448,17 @@ static int upload(ctgb_plan* p) {
     const double gh = split_hi(gam), bi = std::floor(beta);
     lg[4 * i] = gh; lg[4 * i + 1] = gam - gh; lg[4 * i + 2] = bi; lg[4 * i + 3] = beta - bi;
     ls[i] = sigma;
-    const double ah = split_hi(alpha), sh = split_hi(sigma);
+    // Line map x(k) = alpha + sigma*k. The high parts are rounded to multiples
+    // of one power of two qg, chosen so that every value alpha_hi + sigma_hi*k
+    // (k = 0 .. K, the line's pixel edges) is a multiple of qg below 2^p qg in
+    // magnitude, p the precision of T: that sum is then exact in T and the
+    // image gather forms it with one FMA. The low parts are the remainders
+    // (at most qg/2 each), summed by a second FMA to ~2^-38 of the coordinate
+    // in fp32.
+    const int K = (g.flags[i / L] & 1) ? g.W : g.H;
+    const double M = std::max({std::fabs(alpha), std::fabs(alpha + sigma * K), sigma * K});
+    const double qg = std::ldexp(1.0, std::ilogb(M) + 2 - std::numeric_limits<T>::digits);
+    const double ah = std::nearbyint(alpha / qg) * qg, sh = std::nearbyint(sigma / qg) * qg;
     lp[4 * i] = ah; lp[4 * i + 1] = alpha - ah; lp[4 * i + 2] = sh; lp[4 * i + 3] = sigma - sh;
   }
   for (int r = 0; r < g.H; ++r) rowc[r] = (g.height / 2 - r - 0.5) * g.dImg;
@@ -1519,7 +1540,7 @@ static size_t workspace_bytes(const ctgb_plan* p, int op, int batch) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T)
     return al(G * g.H * (size_t)round8(g.W) * sb * es) + al(G * g.W * (size_t)round8(g.H) * sb * es);
-  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es) + pix_parts_bytes(g, op, batch, es);
+  return al(G * g.V * (size_t)padded_cells(g.D) * sb * es) + pix_parts_bytes(g, op, batch, es);
 }
 
 // two straight-line steps are instantiated for every fp32 width (the autotuner
@@ -1541,7 +1562,7 @@ static size_t det_planes_bytes(const HostGeom& g, size_t G, int sb, size_t es) {
 }
 static size_t pix_planes_bytes(const HostGeom& g, size_t G, int sb, size_t es) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  return al(G * g.V * (size_t)((g.D + 3) & ~3) * sb * es);
+  return al(G * g.V * (size_t)padded_cells(g.D) * sb * es);
 }
 
 // The data-term gradient groups slices as projection_t does (both gathers read
