@@ -176,6 +176,9 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+// correctly rounded 1/x (the value of T(1) / x)
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
@@ -623,9 +626,10 @@ __device__ __forceinline__ void report_timeout(int* bad) {
 //
 // Cells are read through records rec[d] = (db_hi[d], db_lo[d], w[d],
 // db_hi[d+1]) and sinogram planes q[qd][d][QW] with plane stride qs; `rec` and
-// `q` point at cell `base`, and only cells in [dlo, dhi) are read. The same
-// code runs on a shared-memory window of the cells (SM) and on the global
-// tables, with identical arithmetic.
+// `q` point at cell `base`; the search stays in [dlo, dhi), and the straight-
+// line steps read at most two padding cells past it. The same code runs on a
+// shared-memory window of the cells (SM, seeded per tile) and on the global
+// tables (seeded by the closed form), with identical arithmetic past the seed.
 
 template <class T, bool SM>
 __device__ __forceinline__ Quad<T> ldrec(const T* p) {
@@ -667,11 +671,28 @@ struct Seed {
 };
 __device__ __forceinline__ Seed load_seed(const float* p) { return {p[0], p[1], p[2], p[3], p[4]}; }
 
-// fp32 seed of the cell holding axis coordinate x, clamped to [dlo, dhi)
-__device__ __forceinline__ int seed_cell(int scan, float xf, const Seed& sd, int dlo, int dhi) {
+// fp32 cell coordinate of axis coordinate x (cell d spans [d, d + 1)), unclamped
+__device__ __forceinline__ float seed_coord(int scan, float xf, const Seed& sd) {
   float u = __fdividef(xf * sd.a, fmaf(xf, sd.c, sd.b));
   if (scan == kFanEA) u = atanf(u);
-  const float cb = fmaf(sd.e, u, sd.d);
+  return fmaf(sd.e, u, sd.d);
+}
+
+// fp32 seed of the cell holding axis coordinate x, clamped to [dlo, dhi)
+__device__ __forceinline__ int seed_cell(int scan, float xf, const Seed& sd, int dlo, int dhi) {
+  return (int)fminf(fmaxf(seed_coord(scan, xf, sd), (float)dlo), (float)(dhi - 1));
+}
+
+// Seed of a staged view: the cell coordinate as a quadratic in x, interpolating
+// the closed form at the ends and the middle of the tile's edge range. Over the
+// few dozen cells a tile spans the map is nearly linear, so the quadratic lands
+// within a small fraction of a cell; like the closed form it only starts the
+// search, so it changes no result.
+struct QuadSeed {
+  float c0, c1, c2;  // cell = c0 + c1 x + c2 x^2
+};
+__device__ __forceinline__ int seed_cell(int, float xf, const QuadSeed& sd, int dlo, int dhi) {
+  const float cb = fmaf(xf, fmaf(xf, sd.c2, sd.c1), sd.c0);
   return (int)fminf(fmaxf(cb, (float)dlo), (float)(dhi - 1));
 }
 
@@ -691,8 +712,8 @@ struct CellSpan {
 // overlaps. Cells past the pixel get weight 0; the straight-line steps may run
 // up to U - 1 cells past dhi, onto the zero-width padding cells of the tables
 // (or of a staged window, which always holds them when it reaches D).
-template <class T, int KIND, int U, bool SM>
-__device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, T kf, const Seed& sd, T sx, T sy,
+template <class T, int KIND, int U, bool SM, class SeedT>
+__device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4, T kf, const SeedT& sd, T sx, T sy,
                                          T pcx, T pcy, const T* __restrict__ rec, int base, int dlo, int dhi,
                                          CellSpan<T, U>& cs) {
   // x = alpha + sigma*k as (xs, xl): the line map's high parts lie on a grid
@@ -729,17 +750,17 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
   if (KIND == kB) {
     if (P.scan == kFanED) {
       const T t = ued_base(sx, sy, pcx, pcy);
-      wv = T(1) / (t * t * sig);
+      wv = rcp_rn(t * t * sig);
     }
-    else if (P.scan == kFanEA) wv = T(1) / (dist2_ea(sx, sy, pcx, pcy) * sig);
-    else wv = T(1) / P.dImg;
+    else if (P.scan == kFanEA) wv = rcp_rn(dist2_ea(sx, sy, pcx, pcy) * sig);
+    else wv = rcp_rn(P.dImg);
   }
 #pragma unroll
   for (int j = 0; j < U; ++j) {
     cs.oj[j] = d + j - base;
     const T w = j == 0 ? w0 : rec[cs.oj[j] * 4 + 2];
-    T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
-    cs.ov[j] = ov > T(0) ? (KIND == kB ? ov * wv : ov) : T(0);
+    const T ov = fmax(fmin(b, w) - fmax(a, T(0)), T(0));
+    cs.ov[j] = KIND == kB ? ov * wv : ov;
     a -= w;
     b -= w;
   }
@@ -768,7 +789,7 @@ __device__ __forceinline__ void pix_accum(const CellSpan<T, U>& cs, const T* __r
   T a = cs.a, b = cs.b;
   for (int d = cs.d; b > T(0) && d < dhi; ++d) {
     const T w = rec[(d - base) * 4 + 2];
-    T ov = (b < w ? b : w) - (a > T(0) ? a : T(0));
+    T ov = fmin(b, w) - fmax(a, T(0));
     if (ov > T(0)) {
       if (KIND == kB) ov *= cs.wv;
 #pragma unroll
@@ -785,8 +806,8 @@ __device__ __forceinline__ void pix_accum(const CellSpan<T, U>& cs, const T* __r
 }
 
 // one view's contribution to one pixel, accumulated into blk
-template <class T, int SB, int KIND, int U, bool SM>
-__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, T kf, const Seed& sd, T sx, T sy,
+template <class T, int SB, int KIND, int U, bool SM, class SeedT>
+__device__ __forceinline__ void pix_view(const DevPlan<T>& P, const Quad<T>& A4, T kf, const SeedT& sd, T sx, T sy,
                                          T pcx, T pcy, const T* __restrict__ rec, const T* __restrict__ qv, int qs,
                                          int base, int dlo, int dhi, T (&blk)[SB]) {
   CellSpan<T, U> cs;
@@ -886,9 +907,10 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
   constexpr int kSlots = ctgb::kSlots<T, SB>;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
   __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
-  // slot header, two 16-byte words: (window start or -1, flags, first line,
-  // seed a) and seed (b, c, d, e); the source position for the backprojector
-  __shared__ int4 s_hdr[kSlots][2];
+  // slot header: (window cell count or -1, flags, first line, seed c0) and seed
+  // (c1, c2); the source position for the backprojector
+  __shared__ int4 s_hdr[kSlots];
+  __shared__ float2 s_qsd[kSlots];
   __shared__ T s_src[kSlots][2];
   __shared__ int s_bad;
   extern __shared__ __align__(16) unsigned char pix_smem[];
@@ -936,8 +958,9 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
       in.A4[0] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r0 : c0)) * 4);
       in.A4[1] = ld4<T>(P.lp + ((size_t)v * P.L + (xb ? r1 : c1)) * 4);
     };
-    // window start of view v, or -1 if the tile's footprint does not fit
-    auto window = [&](int v, const ViewIn& in, int& l0, int& nl) {
+    // window start of view v, or -1 if the tile's footprint does not fit; qs:
+    // the view's quadratic seed over the tile's edge range
+    auto window = [&](int v, const ViewIn& in, int& l0, int& nl, QuadSeed& qs) {
       if (v >= vend) return -1;
       const bool xb = in.fl & 1;
       int ka, kb;
@@ -947,11 +970,17 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
       T xs[4];
       int d[4];
       T lo_b[4], hi_b[4];
+      // the corner edges' seeds, kept for the quadratic: the extremes of the
+      // edge range are corner edges
+      float xlo = 0.f, xhi = 0.f, flo = 0.f, fhi = 0.f;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const Quad<T>& A4 = in.A4[e & 1];
         xs[e] = add_rn(A4.x, mul_rn(A4.z, T((e & 2) ? kb : ka)));
-        d[e] = seed_cell(P.scan, (float)xs[e], in.sd, 0, D);
+        const float xf = (float)xs[e], fe = seed_coord(P.scan, xf, in.sd);
+        if (e == 0 || xf < xlo) { xlo = xf; flo = fe; }
+        if (e == 0 || xf > xhi) { xhi = xf; fhi = fe; }
+        d[e] = (int)fminf(fmaxf(fe, 0.f), (float)(D - 1));
         lo_b[e] = db2v[2 * d[e]];
         hi_b[e] = db2v[2 * d[e] + 2];
       }
@@ -967,15 +996,24 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
         dmin = min(dmin, dd);
         dmax = max(dmax, dd);
       }
+      {  // quadratic through the ends and the middle of [xlo, xhi]
+        const float h = 0.5f * (xhi - xlo), xm = xlo + h;
+        const float fm = seed_coord(P.scan, xm, in.sd), ih = __fdividef(0.5f, h);
+        const float s1 = (fhi - flo) * ih, s2 = ((fhi - fm) - (fm - flo)) * ih * __fdividef(1.f, h);
+        qs.c2 = s2;
+        qs.c1 = fmaf(-2.f * s2, xm, s1);
+        qs.c0 = fmaf(fmaf(s2, xm, -s1), xm, fm);
+      }
       // two cells of margin, or up to the second padding cell past D
       const int lo = max(0, dmin - 2) & ~3;
       const int hi = min(D + 1, dmax + 2);
       return hi < lo + kWin ? lo : -1;
     };
     ViewIn cur, nxt;
+    QuadSeed qsd{0.f, 0.f, 0.f};
     int ws, l0 = 0, nl = 0;
     load_in(vbeg + lane, cur);
-    ws = window(vbeg + lane, cur, l0, nl);
+    ws = window(vbeg + lane, cur, l0, nl, qsd);
     // Views issued so far (header written and the slot's full barrier armed).
     // Before use u of a slot the producer waits until the consumers released
     // use u - 1 (empty) and until use u - 1's copies landed (full), so at most
@@ -1006,13 +1044,10 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
         const int nlj = __shfl_sync(0xffffffffu, nl, j);
         const bool staged = wsj >= 0;
         if (lane == j) {
-          // staged: the window's cell count and the seed shifted to window-relative
-          // cells, so that consumers index the slot directly (the seed only starts
-          // the search for the bracketing cell, so its rounding never matters)
-          s_hdr[slot][0] = make_int4(staged ? min(kWin, D - ws) : -1, cur.fl, l0, __float_as_int(cur.sd.a));
-          s_hdr[slot][1] = make_int4(__float_as_int(cur.sd.b), __float_as_int(cur.sd.c),
-                                     __float_as_int(staged ? cur.sd.d - (float)ws : cur.sd.d),
-                                     __float_as_int(cur.sd.e));
+          // staged: the window's cell count and the quadratic seed shifted to
+          // window-relative cells, so that consumers index the slot directly
+          s_hdr[slot] = make_int4(staged ? min(kWin, D - ws) : -1, cur.fl, l0, __float_as_int(qsd.c0 - (float)ws));
+          s_qsd[slot] = make_float2(qsd.c1, qsd.c2);
           s_src[slot][0] = cur.sx;
           s_src[slot][1] = cur.sy;
         }
@@ -1039,7 +1074,7 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
       }
       if (j < nv) break;  // stopped after a timeout
       cur = nxt;
-      ws = window(vbeg + ub + 32 + lane, cur, l0, nl);
+      ws = window(vbeg + ub + 32 + lane, cur, l0, nl, qsd);
     }
     // Normally the consumers wait on every phase issued. After a timeout, wait
     // for the last issued phase of every slot (the only one that can still be
@@ -1099,11 +1134,10 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
         for (int s = 0; s < SB; ++s) blk[p][s] = T(0);
     }
     if (any) {
-      const int4 h0 = ok ? s_hdr[slot][0] : make_int4(-1, 0, 0, 0);
+      const int4 h0 = ok ? s_hdr[slot] : make_int4(-1, 0, 0, 0);
       if (h0.x >= 0) {
-        const int4 h1 = s_hdr[slot][1];
-        const Seed sd{__int_as_float(h0.w), __int_as_float(h1.x), __int_as_float(h1.y), __int_as_float(h1.z),
-                      __int_as_float(h1.w)};
+        const float2 h1 = s_qsd[slot];
+        const QuadSeed sd{__int_as_float(h0.w), h1.x, h1.y};
         const bool xb = h0.y & 1;
         const unsigned char* sl = slots + slot * S::kBytes;
         const T* sq = reinterpret_cast<const T*>(sl);
