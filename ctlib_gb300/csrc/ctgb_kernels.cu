@@ -720,27 +720,30 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
   // that makes alpha_hi + sigma_hi*k exact for every edge of the line
   const T xs = fma(A4.z, kf, A4.x);
   const T xl = fma(A4.w, kf, A4.y);
-  // seed the cell and correct it: db_hi[d] <= xs < db_hi[d+1], d in [dlo, dhi)
+  // The cell: db_hi[d] <= xs < db_hi[d+1], d in [dlo, dhi), then one cell back
+  // if the offset of the edge into it, taken between the two nearby pairs, is
+  // negative. The seed is almost always that cell with a non-negative offset,
+  // which one test confirms; otherwise the search walks from the seed.
   int d = seed_cell(P.scan, (float)xs, sd, dlo, dhi);
   Quad<T> rd = ldrec<T, SM>(rec + (d - base) * 4);
-  if (d > dlo && xs < rd.x) {
-    do {
-      --d;
-      rd = ldrec<T, SM>(rec + (d - base) * 4);
-    } while (d > dlo && xs < rd.x);
-  } else if (d < dhi - 1 && rd.w <= xs) {
-    do {
-      ++d;
-      rd = ldrec<T, SM>(rec + (d - base) * 4);
-    } while (d < dhi - 1 && rd.w <= xs);
-  }
-  // offset of the edge into its cell, from the two nearby pairs
   T a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
   T w0 = rd.z;
-  if (a < T(0) && d > dlo) {
-    --d;
-    w0 = rec[(d - base) * 4 + 2];
-    a += w0;
+  if (!(rd.x <= xs && xs < rd.w && a >= T(0))) {
+    while (d > dlo && xs < rd.x) {
+      --d;
+      rd = ldrec<T, SM>(rec + (d - base) * 4);
+    }
+    while (d < dhi - 1 && rd.w <= xs) {  // after a step down, rd.w > xs already
+      ++d;
+      rd = ldrec<T, SM>(rec + (d - base) * 4);
+    }
+    a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
+    w0 = rd.z;
+    if (a < T(0) && d > dlo) {
+      --d;
+      w0 = rec[(d - base) * 4 + 2];
+      a += w0;
+    }
   }
   const T sig = A4.z + A4.w;
   T b = a + sig;
@@ -787,6 +790,7 @@ __device__ __forceinline__ void pix_accum(const CellSpan<T, U>& cs, const T* __r
       for (int i = 0; i < QW; ++i) blk[qd * QW + i] = fma(cs.ov[j], qq[j][i], blk[qd * QW + i]);
   }
   T a = cs.a, b = cs.b;
+  if (!(b > T(0))) return;
   for (int d = cs.d; b > T(0) && d < dhi; ++d) {
     const T w = rec[(d - base) * 4 + 2];
     T ov = fmin(b, w) - fmax(a, T(0));
@@ -872,16 +876,25 @@ struct PixSlot {
   static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
 };
 
+// CTAs per SM of the staged image gather: four at one fp32 slice per thread,
+// whose sums fit 56 registers and whose small slots leave room for four CTAs'
+// rings (more warps to hide the shared-memory latency of an issue-bound loop);
+// three otherwise (72 registers).
+template <class T, int SB>
+constexpr int kPixCtas = (sizeof(T) == 4 && SB == 1) ? 4 : 3;
+
 // Views in flight per CTA: as many slots as fit beside the Kahan sums of 8 row
-// warps with three CTAs per SM (74 KB of dynamic shared memory each, leaving
-// room for the static arrays and the per-CTA reserve), at most 16. The ring
-// has to cover the time from a slot's release by the slowest row warp to its
-// refill landing; the few-slice slots are small, so those rings get deep (16
-// slots for one to four slices per thread, 11 for eight, 7 for sixteen).
+// warps with kPixCtas CTAs per SM (228 KB of shared memory per SM, less 2 KB per
+// CTA for the static arrays and the per-CTA reserve: 74 KB of dynamic shared
+// memory each at three CTAs, 55 KB at four), at most 16. The ring has to cover
+// the time from a slot's release by the slowest row warp to its refill
+// landing; the few-slice slots are small, so those rings get deep (16 slots
+// for one to four slices per thread, 11 for eight, 7 for sixteen).
 template <class T, int SB>
 constexpr int kSlots = [] {
   constexpr int acc = 2 * kPixRows<SB> * SB * 256 * (int)sizeof(T);
-  constexpr int n = (74 * 1024 - acc - 1024) / PixSlot<T, SB>::kBytes;
+  constexpr int budget = 228 * 1024 / kPixCtas<T, SB> - 2048;
+  constexpr int n = (budget - acc - 1024) / PixSlot<T, SB>::kBytes;
   return n > 16 ? 16 : (n < 4 ? 4 : n);
 }();
 
@@ -1200,7 +1213,7 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
 }
 
 template <class T, int SB, int KIND, int U, bool SV = false, int PX = 1, bool PLAIN = false>
-__global__ void __launch_bounds__(288, 3) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
+__global__ void __launch_bounds__(288, (kPixCtas<T, SB>)) k_pix_gather(DevPlan<T> P, const T* __restrict__ q,
                                                        T* __restrict__ img, T* __restrict__ parts, int B,
                                                        T out_mul, T out_div, int nsplit) {
   pix_gather_cta<T, SB, KIND, U, SV, PX, PLAIN>(P, q, img, parts, B, out_mul, out_div, nsplit, blockIdx.x, blockIdx.y,
@@ -1972,7 +1985,7 @@ __global__ void __launch_bounds__(256) k_rag_sino_rows(const __grid_constant__ R
 // results are the same bit for bit. Sinogram planes [V][Dp] per slice at
 // off_q, partial images [parts][H][W] at off_parts.
 template <class T, int KIND>
-__global__ void __launch_bounds__(32 * (kRagPixWarps + 1), 3)
+__global__ void __launch_bounds__(32 * (kRagPixWarps + 1), (kPixCtas<T, 1>))
     k_rag_pix_gather(const __grid_constant__ RaggedPlans<T> rp, const RPixTask* __restrict__ tasks,
                      const __grid_constant__ RaggedIO<T> io, unsigned char* ws, const size_t* __restrict__ off_q,
                      const size_t* __restrict__ off_parts, int fbp_scale) {
