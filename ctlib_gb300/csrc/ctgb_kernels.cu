@@ -678,9 +678,10 @@ __device__ __forceinline__ float seed_coord(int scan, float xf, const Seed& sd) 
   return fmaf(sd.e, u, sd.d);
 }
 
-// fp32 seed of the cell holding axis coordinate x, clamped to [dlo, dhi)
+// fp32 seed of the cell holding axis coordinate x, clamped to [dlo, dhi) (the
+// conversion saturates, and maps NaN to 0)
 __device__ __forceinline__ int seed_cell(int scan, float xf, const Seed& sd, int dlo, int dhi) {
-  return (int)fminf(fmaxf(seed_coord(scan, xf, sd), (float)dlo), (float)(dhi - 1));
+  return min(max(__float2int_rz(seed_coord(scan, xf, sd)), dlo), dhi - 1);
 }
 
 // Seed of a staged view: the cell coordinate as a quadratic in x, interpolating
@@ -692,8 +693,7 @@ struct QuadSeed {
   float c0, c1, c2;  // cell = c0 + c1 x + c2 x^2
 };
 __device__ __forceinline__ int seed_cell(int, float xf, const QuadSeed& sd, int dlo, int dhi) {
-  const float cb = fmaf(xf, fmaf(xf, sd.c2, sd.c1), sd.c0);
-  return (int)fminf(fmaxf(cb, (float)dlo), (float)(dhi - 1));
+  return min(max(__float2int_rz(fmaf(xf, fmaf(xf, sd.c2, sd.c1), sd.c0)), dlo), dhi - 1);
 }
 
 // Where one view meets one pixel: the pixel's first U cells (offsets oj from
@@ -890,9 +890,9 @@ constexpr int kPixCtas = (sizeof(T) == 4 && SB == 1) ? 4 : 3;
 // the time from a slot's release by the slowest row warp to its refill
 // landing; the few-slice slots are small, so those rings get deep (16 slots
 // for one to four slices per thread, 11 for eight, 7 for sixteen).
-template <class T, int SB>
+template <class T, int SB, int PX = kPixRows<SB>>
 constexpr int kSlots = [] {
-  constexpr int acc = 2 * kPixRows<SB> * SB * 256 * (int)sizeof(T);
+  constexpr int acc = 2 * PX * SB * 256 * (int)sizeof(T);
   constexpr int budget = 228 * 1024 / kPixCtas<T, SB> - 2048;
   constexpr int n = (budget - acc - 1024) / PixSlot<T, SB>::kBytes;
   return n > 16 ? 16 : (n < 4 ? 4 : n);
@@ -917,7 +917,7 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
   constexpr int QW = Planes<SB>::QW, NQ = Planes<SB>::NQ;
   using S = PixSlot<T, SB>;
   constexpr int kWin = S::kWin;
-  constexpr int kSlots = ctgb::kSlots<T, SB>;
+  constexpr int kSlots = ctgb::kSlots<T, SB, PX>;
   static_assert(NQ + 2 <= 32, "one producer lane per copy");
   __shared__ __align__(8) unsigned long long s_full[kSlots], s_empty[kSlots];
   // slot header: (window cell count or -1, flags, first line, seed c0) and seed
@@ -1457,6 +1457,7 @@ struct ctgb_plan {
   // optional events recorded right before and after each gather kernel on the
   // launch stream (ctgb_plan_set_kernel_events), to time that kernel alone
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  int sms = 152;        // multiprocessors of the plan's device
   void* dev = nullptr;  // one allocation holding all tables
   ctgb::DevPlan<float> pf{};
   ctgb::DevPlan<double> pd{};
@@ -1532,6 +1533,7 @@ static int upload(ctgb_plan* p) {
   float* invf = reinterpret_cast<float*>(host.data() + off_inv);
   for (size_t j = 0; j < g.inv.size(); ++j) invf[j] = (float)g.inv[j];
   CTGB_CUDA(cudaSetDevice(p->device));
+  CTGB_CUDA(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
   CTGB_CUDA(cudaMalloc(&p->dev, off));
   CTGB_CUDA(cudaMemcpy(p->dev, host.data(), off, cudaMemcpyHostToDevice));
   unsigned char* b = static_cast<unsigned char*>(p->dev);
@@ -1669,6 +1671,18 @@ static int launch_det(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   return CTGB_OK;
 }
 
+template <class T, int SB, int PX>
+static int launch_pix_rows(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, T* y, int batch, const T* qb,
+                           T* parts, int nsplit, cudaStream_t st);
+
+// Four pixel rows per consumer thread are built for one fp32 slice per thread:
+// they share each warp's per-view costs between twice the pixels of two rows,
+// and are taken when the grid still fills two waves (16 x 16 tiles x 8 view
+// parts for one 512^2 slice of 1152 views: A^T 0.97 -> 0.85 ms), not on small
+// images (parallel 256^2, 360 views: 128 CTAs, 0.14 -> 0.18 ms).
+template <class T, int SB>
+constexpr bool kWideBuilt = sizeof(T) == 4 && SB == 1;
+
 // Staged image gather (A^T, B, fbp's backprojection, single-view B) from the
 // sinogram planes qb; unless `planes_ready`, qb is first filled from x (re-layout,
 // or the ramp filter for fbp). `parts` holds the partial images of the view
@@ -1704,19 +1718,36 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
     k_layout_sino<T, SB><<<nb, tb, 0, st>>>(x, qb, P.flags, op == CTGB_OP_PROJECTION_T ? P.fq : nullptr, batch,
                                            g.V, g.D, P.Dp, G, pf);
   }
+  // single-view backprojection writes each view's image on its own, so its views
+  // split over any number of CTAs with no adds: 8 parts shorten the CTAs of a
+  // grid that is only ~2 waves deep (7.62 to 6.85 ms for 16 x 512^2, 1152 views)
+  const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? std::min(8, g.V) : view_split(g.V);
+  if constexpr (kWideBuilt<T, SB>) {
+    const int wpc = p->warps[sched];
+    const long long ctas = (long long)((g.W + 31) / 32) * ((g.H + 4 * wpc - 1) / (4 * wpc)) * G * nsplit;
+    if (ctas >= 2LL * p->sms * kPixCtas<T, SB>)
+      return launch_pix_rows<T, SB, 4>(p, P, op, sched, y, batch, qb, parts, nsplit, st);
+  }
+  return launch_pix_rows<T, SB, kPixRows<SB>>(p, P, op, sched, y, batch, qb, parts, nsplit, st);
+}
+
+// The staged image gather at PX pixel rows per consumer thread, then the sum
+// of its view parts.
+template <class T, int SB, int PX>
+static int launch_pix_rows(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, T* y, int batch, const T* qb,
+                           T* parts, int nsplit, cudaStream_t st) {
+  const int G = (batch + SB - 1) / SB;
+  const HostGeom& g = p->geom;
+  const bool plain = kPlainBuilt<T> && p->plain && op != CTGB_OP_BACKPROJECTION_SV;
   const int wpc = p->warps[sched];  // consumer warps (PX pixel rows each) + one producer warp
-  constexpr int PX = kPixRows<SB>;
   dim3 grid((g.W + 31) / 32, (g.H + wpc * PX - 1) / (wpc * PX), G);
   const int nt = 32 * (wpc + 1);
-  const size_t smem = (size_t)2 * PX * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots<T, SB> * PixSlot<T, SB>::kBytes;
+  const size_t smem =
+      (size_t)2 * PX * SB * (32 * wpc) * sizeof(T) + (size_t)kSlots<T, SB, PX> * PixSlot<T, SB>::kBytes;
   auto launch = [&](auto kern, T mul, T div) -> int {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(CTGB_ERR_CUDA, std::string("image gather smem: ") + cudaGetErrorString(e));
-    // single-view backprojection writes each view's image on its own, so its views
-    // split over any number of CTAs with no adds: 8 parts shorten the CTAs of a
-    // grid that is only ~2 waves deep (7.62 to 6.85 ms for 16 x 512^2, 1152 views)
     const bool sv = op == CTGB_OP_BACKPROJECTION_SV;
-    const int nsplit = sv ? std::min(8, g.V) : view_split(g.V);
     if (p->ev_start) cudaEventRecord(p->ev_start, st);
     kern<<<dim3(grid.x, grid.y, grid.z * nsplit), nt, smem, st>>>(P, qb, y, parts, batch, mul, div, nsplit);
     if (p->ev_stop) cudaEventRecord(p->ev_stop, st);
@@ -1904,10 +1935,13 @@ struct RPixTask {
   int slice, bx, by, part;
 };
 
-// tile rows per CTA of the ragged image gather: 8 row warps, two pixel rows each
-// (the per-slice calls' layout for one slice per thread with 8 warps)
+// tile rows per CTA of the ragged image gather: 8 row warps of kRagPX pixel rows
 constexpr int kRagPixWarps = 8;
-constexpr int kRagPixRows = kRagPixWarps * kPixRows<1>;
+// pixel rows per consumer thread of a ragged tile: four, as a one-slice call
+// takes on large images (the ragged launch's task list always fills the GPU;
+// one launch per stage on 96 mixed slices: 169 -> 157 ms against two rows)
+constexpr int kRagPX = 4;
+constexpr int kRagPixRows = kRagPixWarps * kRagPX;
 
 template <class T>
 __global__ void __launch_bounds__(256) k_rag_transpose(const __grid_constant__ RaggedPlans<T> rp,
@@ -1991,7 +2025,7 @@ __global__ void __launch_bounds__(32 * (kRagPixWarps + 1), (kPixCtas<T, 1>))
                      const size_t* __restrict__ off_parts, int fbp_scale) {
   const RPixTask t = tasks[blockIdx.x];
   const DevPlan<T>& P = rp.p[t.slice];
-  pix_gather_cta<T, 1, KIND, kTwoStep<T, 1> ? 2 : 3, false, kPixRows<1>, false>(
+  pix_gather_cta<T, 1, KIND, kTwoStep<T, 1> ? 2 : 3, false, kRagPX, false>(
       P, reinterpret_cast<const T*>(ws + off_q[t.slice]), io.out[t.slice],
       reinterpret_cast<T*>(ws + off_parts[t.slice]), 1, fbp_scale ? P.dAng : T(1), fbp_scale ? T(2) : T(1),
       view_split(P.V), t.bx, t.by, t.part);
@@ -2229,8 +2263,8 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
   r->off_sino = reinterpret_cast<const size_t*>(base + o_os);
   r->off_parts = reinterpret_cast<const size_t*>(base + o_op);
   RaggedStage* st[6] = {&r->transpose, &r->detg, &r->rows, &r->pixg, &r->ramp, &r->combine};
-  constexpr int kPX = kPixRows<1>;
-  r->pix_smem = (size_t)2 * kPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots<T, 1> * PixSlot<T, 1>::kBytes;
+  r->pix_smem =
+      (size_t)2 * kRagPX * 1 * (32 * kRagPixWarps) * es + (size_t)kSlots<T, 1, kRagPX> * PixSlot<T, 1>::kBytes;
   for (const void* f : {(const void*)k_rag_pix_gather<T, kAt>, (const void*)k_rag_pix_gather<T, kB>})
     CTGB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r->pix_smem));
   const size_t ramp_smem = ramp_smem_elems(r->maxD, 1) * es;
