@@ -570,9 +570,8 @@ def run_ours(args):
 
     # kernels of this package per timed step: image layout + detector gather,
     # sinogram layout + image gather, and the sum of the image gather's view
-    # parts when it splits the views (V / 128 parts up to 8, one below 256 views:
-    # view_split in csrc/ctgb_kernels.cu)
-    launches_per_step = 4 + (1 if V >= 256 else 0)
+    # parts when it splits the views
+    launches_per_step = 4 + (1 if _view_split(V, W * H) > 1 else 0)
 
     # -- roofline of the dominant kernel -------------------------------------
     ta, tat = statistics.mean(t_a), statistics.mean(t_at)
@@ -805,11 +804,14 @@ def run_unrolled(args):
 
     # operator launches per step, counted on one untimed step
     calls = [0]
+    image_gathers = [0]  # calls whose kernel is the image gather (A^T, B, fbp)
     if counted is None:
         orig = ag._run
 
         def counting(op, x, plan):
             calls[0] += 1
+            if op in (ag.N.OP_PROJECTION_T, ag.N.OP_BACKPROJECTION, ag.N.OP_FBP):
+                image_gathers[0] += 1
             return orig(op, x, plan)
         ag._run = counting
         try:
@@ -879,8 +881,10 @@ def run_unrolled(args):
                         "sm_103a (oracle/ref_cuda.py), the same checkpointed recursion")
     else:
         line["path"] = "ctlib_gb300.recon.unrolled_gd through ctlib_gb300.autograd (projection <-> projection_t)"
-        # each operator call launches a layout kernel and a gather kernel
-        line["gpu_launches"] = 2 * ops_per_step * args.steps
+        # each operator call launches a layout kernel and a gather kernel, and an
+        # image gather that splits its views also the sum of the parts
+        split = _view_split(V, W * H) > 1
+        line["gpu_launches"] = (2 * ops_per_step + (image_gathers[0] if split else 0)) * args.steps
         peak = _fp32_peak(dev)
         model_peak = peak["lane_ops_per_s"] / 8.0
         line["roofline_fp32"] = {"achieved": value, "peak": model_peak, "unit": "ray-updates/s",
@@ -890,6 +894,13 @@ def run_unrolled(args):
         line["cpu_baseline"] = _cpu_baseline(w)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _view_split(views: int, pixels: int) -> int:
+    """View parts of the image gather (view_split in csrc/ctgb_kernels.cu)."""
+    if pixels <= (1 << 17):
+        return 1 if views < 80 else min(8, views // 40)
+    return 1 if views < 256 else (8 if views >= 1024 else views // 128)
 
 
 def _kernel_times(plan, steps, flush, stream, run_a, run_at):

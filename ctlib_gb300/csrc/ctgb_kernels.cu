@@ -834,13 +834,19 @@ __device__ __forceinline__ void pix_view_global(const DevPlan<T>& P, int v, int 
 // Parts per tile of the staged image gather: a tile's views are split into
 // consecutive parts of at least 128 views, up to 8, each part its own CTA.
 // Shorter CTAs fill the last wave of a grid that is only a few waves deep (one
-// 512^2 slice is 1024 tile halves, 2.2 waves of 456 resident CTAs; 16 slices
-// are 4.5 waves). Each part writes its scaled sum to its own partial image and
-// k_combine_parts adds the parts in order, from zero, so the result does not
-// depend on which CTA finishes first. The split depends on V alone, never on
+// 512^2 slice of 1152 views is 2048 CTAs, 3.4 waves of 608 resident ones).
+// Small images (at most 2^17 pixels) have few tiles, so their views split
+// finer, into parts of at least 40 views (one 256^2 slice is 128 tiles of
+// 32 x 16 pixels: with 360 views, 1024 CTAs instead of 256). Each part writes
+// its scaled sum to its own partial image and k_combine_parts adds the parts
+// in order, from zero, so the result does not depend on which CTA finishes
+// first. The split depends on the plan alone (views and image size), never on
 // the batch or the schedule, so every schedule gives the same result bit for
 // bit; the ragged path sums the same parts in the same order and matches too.
-__host__ __device__ __forceinline__ int view_split(int views) { return views < 256 ? 1 : (views >= 1024 ? 8 : views / 128); }
+__host__ __device__ __forceinline__ int view_split(int views, long long pixels) {
+  if (pixels <= (1 << 17)) return views < 80 ? 1 : min(8, views / 40);
+  return views < 256 ? 1 : (views >= 1024 ? 8 : views / 128);
+}
 
 // Staged image gather. A CTA is a 32 x (R * PX) pixel tile plus one producer
 // warp: R consumer warps, lane = column, and warp w owns rows w, w + R, ...,
@@ -902,7 +908,7 @@ constexpr int kSlots = [] {
 // sum goes to its own image, img[slice][view][row][col], with no sum over views.
 //
 // nsplit: blockIdx.z = slice group * nsplit + part, and part p takes views
-// [V*p/nsplit, V*(p+1)/nsplit). Summing operators use view_split(V) parts:
+// [V*p/nsplit, V*(p+1)/nsplit). Summing operators use view_split(V, W*H) parts:
 // with one, the CTA writes the output; with more, part p writes its scaled sum
 // to partial image p of `parts` ([nsplit][B][H][W]) and k_combine_parts adds
 // them. SV writes every view's image directly, so it takes any number of parts
@@ -1576,7 +1582,7 @@ static size_t esize(int dtype) { return dtype == 0 ? 4 : 8; }
 // partial images of the staged image gather's view parts (none for one part
 // or for single-view backprojection, which writes each view's image directly)
 static size_t pix_parts_bytes(const HostGeom& g, int op, int batch, size_t es) {
-  const int np = view_split(g.V);
+  const int np = view_split(g.V, (long long)g.W * g.H);
   if (np == 1 || op == CTGB_OP_BACKPROJECTION_SV) return 0;
   return ((size_t)np * batch * g.H * g.W * es + 255) & ~(size_t)255;
 }
@@ -1721,7 +1727,7 @@ static int launch_pix(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched
   // single-view backprojection writes each view's image on its own, so its views
   // split over any number of CTAs with no adds: 8 parts shorten the CTAs of a
   // grid that is only ~2 waves deep (7.62 to 6.85 ms for 16 x 512^2, 1152 views)
-  const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? std::min(8, g.V) : view_split(g.V);
+  const int nsplit = op == CTGB_OP_BACKPROJECTION_SV ? std::min(8, g.V) : view_split(g.V, (long long)g.W * g.H);
   if constexpr (kWideBuilt<T, SB>) {
     const int wpc = p->warps[sched];
     const long long ctas = (long long)((g.W + 31) / 32) * ((g.H + 4 * wpc - 1) / (4 * wpc)) * G * nsplit;
@@ -2028,7 +2034,7 @@ __global__ void __launch_bounds__(32 * (kRagPixWarps + 1), (kPixCtas<T, 1>))
   pix_gather_cta<T, 1, KIND, kTwoStep<T, 1> ? 2 : 3, false, kRagPX, false>(
       P, reinterpret_cast<const T*>(ws + off_q[t.slice]), io.out[t.slice],
       reinterpret_cast<T*>(ws + off_parts[t.slice]), 1, fbp_scale ? P.dAng : T(1), fbp_scale ? T(2) : T(1),
-      view_split(P.V), t.bx, t.by, t.part);
+      view_split(P.V, (long long)P.W * P.H), t.bx, t.by, t.part);
 }
 
 // k_combine_parts over the slices whose views were split: task (slice, chunk
@@ -2043,7 +2049,7 @@ __global__ void __launch_bounds__(256) k_rag_combine(const __grid_constant__ Rag
     const RTask tk = tasks[t];
     const DevPlan<T>& P = rp.p[tk.slice];
     const size_t n = (size_t)P.H * P.W;
-    const int np = view_split(P.V);
+    const int np = view_split(P.V, (long long)P.W * P.H);
     const T* parts = reinterpret_cast<const T*>(ws + off_parts[tk.slice]);
     const size_t end = min(n, (size_t)(tk.a + 1) * kCombineChunk);
     for (size_t i = (size_t)tk.a * kCombineChunk + threadIdx.x; i < end; i += blockDim.x) {
@@ -2201,7 +2207,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     dp[i] = plan_of<T>(plans[i]);
     hp->p[i] = dp[i];
     const int Dp = dp[i].Dp;
-    const int np = view_split(g.V);
+    const int np = view_split(g.V, (long long)g.W * g.H);
     oi[i] = r->ws_img;
     r->ws_img += al((size_t)g.H * g.W * es);
     os[i] = r->ws_sino;

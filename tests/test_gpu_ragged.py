@@ -30,7 +30,7 @@ def _slices():
             para_options(90, 67, 32, 48, 1.0, 1.1, 0.1, math.pi / 90, 0.4),
             para_options(12, 128, 96, 96, 1.0, 1.2, 0.0, math.pi / 12, 0.0),
             fan_options(128, 256, 96, 80, 1.5, 2.5, 0.0, tp / 128, 595.0, 490.6, 0.0, FAN_ED),
-            # enough views for the image gather to split them into parts (4 and 8),
+            # enough views for the image gather to split them into 8 parts,
             # whose partial images a combine stage adds
             fan_options(520, 180, 40, 56, 1.0, 2.0, 0.1, tp / 520, 150.0, 100.0, 0.2, FAN_ED),
             para_options(1100, 80, 32, 32, 1.0, 1.0, 0.0, math.pi / 1100, 0.0)]
