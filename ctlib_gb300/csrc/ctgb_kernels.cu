@@ -1040,56 +1040,82 @@ __device__ __forceinline__ void pix_gather_cta(const DevPlan<T>& P, const T* __r
     // (here or in a consumer, s_bad), the producer issues nothing more: no
     // header, arrive or copy, since an arrive on a phase still waiting for its
     // bytes would exceed that phase's expected count.
+    // Views go out in rounds of kRound: the lanes of a round's views wait for
+    // their slots, write their headers and arm their full barriers side by
+    // side, then kCopies lanes per view issue its copies, so that a round costs
+    // the serial steps of one view. (One view per step left the row warps
+    // waiting for their slots 28% of the time at 16 slices per thread: the
+    // producer, one warp among the SM's busy row warps, could not keep the
+    // ring ahead.)
+    constexpr int kCopies = NQ + 2;
+    constexpr int kRound = [] {
+      int r = 4;
+      if (32 / kCopies < r) r = 32 / kCopies;
+      if (kSlots / 2 < r) r = kSlots / 2;
+      return r;
+    }();
+    static_assert(kRound >= 1 && kRound * kCopies <= 32, "one lane per copy of a round");
     int issued = 0;
     for (int ub = 0; ub < NV; ub += 32) {
       load_in(vbeg + ub + 32 + lane, nxt);  // in flight during this batch's copies
       const int nv = min(32, NV - ub);
+      const int slot_m = (ub + lane) % kSlots, use_m = (ub + lane) / kSlots;  // this lane's view
+      const bool staged_m = ws >= 0;
       int j = 0;
-      for (; j < nv; ++j) {
-        const int vj = vbeg + ub + j, slot = (ub + j) % kSlots, use = (ub + j) / kSlots;
+      for (; j < nv; j += kRound) {
+        const int ng = min(kRound, nv - j);
+        const bool mine = lane >= j && lane < j + ng;
         int go = 1;
-        if (lane == 0) {
+        if (mine) {
           if (ld_volatile(s_bad)) {
             go = 0;
-          } else if (use > 0 && !(mbar_wait(&s_empty[slot], (use - 1) & 1, P.wait_ns) &&
-                                  mbar_wait(&s_full[slot], (use - 1) & 1, P.wait_ns))) {
+          } else if (use_m > 0 && !(mbar_wait(&s_empty[slot_m], (use_m - 1) & 1, P.wait_ns) &&
+                                    mbar_wait(&s_full[slot_m], (use_m - 1) & 1, P.wait_ns))) {
             report_timeout(&s_bad);
             go = 0;
           }
         }
-        if (!__shfl_sync(0xffffffffu, go, 0)) break;
-        const int wsj = __shfl_sync(0xffffffffu, ws, j);
-        const int l0j = __shfl_sync(0xffffffffu, l0, j);
-        const int nlj = __shfl_sync(0xffffffffu, nl, j);
-        const bool staged = wsj >= 0;
-        if (lane == j) {
+        if (!__all_sync(0xffffffffu, go)) break;
+        if (mine) {
           // staged: the window's cell count and the quadratic seed shifted to
           // window-relative cells, so that consumers index the slot directly
-          s_hdr[slot] = make_int4(staged ? min(kWin, D - ws) : -1, cur.fl, l0, __float_as_int(qsd.c0 - (float)ws));
-          s_qsd[slot] = make_float2(qsd.c1, qsd.c2);
-          s_src[slot][0] = cur.sx;
-          s_src[slot][1] = cur.sy;
+          s_hdr[slot_m] = make_int4(staged_m ? min(kWin, D - ws) : -1, cur.fl, l0, __float_as_int(qsd.c0 - (float)ws));
+          s_qsd[slot_m] = make_float2(qsd.c1, qsd.c2);
+          s_src[slot_m][0] = cur.sx;
+          s_src[slot_m][1] = cur.sy;
         }
         __syncwarp();
-        ++issued;
-        if (!staged) {
-          if (lane == 0) mbar_arrive(&s_full[slot]);
-          continue;
+        if (mine) {
+          if (staged_m) {
+            const int ncell = min(kWin, Dp - ws);
+            mbar_arrive_expect_tx(&s_full[slot_m],
+                                  (unsigned)((ncell * (NQ * QW + 4) + nl * 4) * (int)sizeof(T)));
+          } else {
+            mbar_arrive(&s_full[slot_m]);
+          }
         }
-        const int ncell = min(kWin, Dp - wsj);
-        const unsigned qbytes = (unsigned)(ncell * QW * sizeof(T));
-        const unsigned rbytes = (unsigned)(ncell * 4 * sizeof(T));
-        const unsigned lbytes = (unsigned)(nlj * 4 * sizeof(T));
-        if (lane == 0) mbar_arrive_expect_tx(&s_full[slot], NQ * qbytes + rbytes + lbytes);
+        issued += ng;
         __syncwarp();
-        unsigned char* sl = slots + (size_t)slot * S::kBytes;
-        if (lane < NQ)
-          bulk_g2s(sl + (size_t)lane * kWin * QW * sizeof(T), qg + (((size_t)vj * NQ + lane) * Dp + wsj) * QW,
-                   qbytes, &s_full[slot]);
-        else if (lane == NQ)
-          bulk_g2s(sl + S::kQBytes, P.rec + ((size_t)vj * Dp + wsj) * 4, rbytes, &s_full[slot]);
-        else if (lane == NQ + 1)
-          bulk_g2s(sl + S::kQBytes + S::kRecBytes, P.lp + ((size_t)vj * P.L + l0j) * 4, lbytes, &s_full[slot]);
+        // copy c of the round's view g on lane g * kCopies + c
+        const int g = lane / kCopies, c = lane - g * kCopies;
+        const int src = j + min(g, ng - 1);
+        const int wsg = __shfl_sync(0xffffffffu, ws, src);
+        const int l0g = __shfl_sync(0xffffffffu, l0, src);
+        const int nlg = __shfl_sync(0xffffffffu, nl, src);
+        if (g < ng && wsg >= 0) {
+          const int ug = ub + j + g, vg = vbeg + ug, slot = ug % kSlots;
+          const int ncell = min(kWin, Dp - wsg);
+          unsigned char* sl = slots + (size_t)slot * S::kBytes;
+          if (c < NQ)
+            bulk_g2s(sl + (size_t)c * kWin * QW * sizeof(T), qg + (((size_t)vg * NQ + c) * Dp + wsg) * QW,
+                     (unsigned)(ncell * QW * sizeof(T)), &s_full[slot]);
+          else if (c == NQ)
+            bulk_g2s(sl + S::kQBytes, P.rec + ((size_t)vg * Dp + wsg) * 4, (unsigned)(ncell * 4 * sizeof(T)),
+                     &s_full[slot]);
+          else
+            bulk_g2s(sl + S::kQBytes + S::kRecBytes, P.lp + ((size_t)vg * P.L + l0g) * 4,
+                     (unsigned)(nlg * 4 * sizeof(T)), &s_full[slot]);
+        }
       }
       if (j < nv) break;  // stopped after a timeout
       cur = nxt;
