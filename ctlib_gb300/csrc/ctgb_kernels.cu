@@ -1969,6 +1969,8 @@ struct RPixTask {
 
 // tile rows per CTA of the ragged image gather: 8 row warps of kRagPX pixel rows
 constexpr int kRagPixWarps = 8;
+// views per CTA (one warp each) of the ragged detector gather
+constexpr int kRagDetWarps = 8;
 // pixel rows per consumer thread of a ragged tile: four, as a one-slice call
 // takes on large images (the ragged launch's task list always fills the GPU;
 // one launch per stage on 96 mixed slices: 169 -> 157 ms against two rows)
@@ -2244,7 +2246,7 @@ static int ragged_build(ctgb_ragged* r, const ctgb_plan* const* plans, int n) {
     const long lines = g.H > g.W ? g.H : g.W;
     for (int a = 0; a < (g.H + 31) / 32; ++a)
       for (int b = 0; b < (g.W + 31) / 32; ++b) tr.push_back({1, {i, a, b}});
-    for (int a = 0; a < (g.V + 7) / 8; ++a)
+    for (int a = 0; a < (g.V + kRagDetWarps - 1) / kRagDetWarps; ++a)
       for (int b = 0; b < (g.D + 31) / 32; ++b) dg.push_back({lines, {i, a, b}});
     for (int a = 0; a < g.V; ++a) {
       rw.push_back({g.D, {i, a, 0}});
@@ -2331,13 +2333,14 @@ static int ragged_run_t(const ctgb_ragged* r, int op, const void* const* in, voi
   if (op == CTGB_OP_PROJECTION || op == CTGB_OP_BACKPROJECTION_T) {
     k_rag_transpose<T><<<r->transpose.grid, 256, 0, st>>>(hp, rt(r->transpose), r->transpose.n, io, w,
                                                           r->off_img);
-    const size_t acc_smem = (size_t)2 * 256 * sizeof(T);
+    const int nt = 32 * kRagDetWarps;
+    const size_t acc_smem = (size_t)2 * nt * sizeof(T);
     if (op == CTGB_OP_PROJECTION)
-      k_rag_det_gather<T, kA><<<r->detg.grid, 256, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
-                                                                   r->off_img);
+      k_rag_det_gather<T, kA><<<r->detg.grid, nt, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
+                                                                  r->off_img);
     else
-      k_rag_det_gather<T, kBt><<<r->detg.grid, 256, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
-                                                                    r->off_img);
+      k_rag_det_gather<T, kBt><<<r->detg.grid, nt, acc_smem, st>>>(hp, rt(r->detg), r->detg.n, io, w,
+                                                                   r->off_img);
   } else {
     if (op == CTGB_OP_FBP) {
       const size_t smem = ramp_smem_elems(r->maxD, 1) * sizeof(T);
