@@ -79,10 +79,14 @@ struct DevPlan {
   int even_taps;      // fbp filter with non-zero even offsets (windowed kernels), besides the centre
   unsigned long long wait_ns;  // limit of each bounded wait in the staged image gather
   T dImg, s2r, dAng, wscale;
+  // at least 1.5 units in the last place of the largest cell boundary (4 used):
+  // db_hi[d+1] - db_hi[d] and w[d] differ by less, so an edge with
+  // xs - db_hi[d] < w[d] - ub_margin lies below db_hi[d+1]
+  T ub_margin;
   const int* flags;   // V
   const T* wsrc;      // V*2   weight source: equal-distance fans (sx, sy) / s2r^2, equal-angle (sx, sy)
   const T* db2;       // V*(D+1)*2  cell boundaries (hi, lo)
-  const T* rec;       // V*Dp*4 cell records (db hi, db lo, width, next db hi); zero past D
+  const T* rec;       // V*Dp*4 cell records (db hi, db lo, width, next cell's width); zero past D
   const T* wd;        // V*D   cell widths
   const T* fq;        // V*D   A / A^T factor
   const T* fbt;       // V*D   EA B^T factor
@@ -625,7 +629,7 @@ __device__ __forceinline__ void report_timeout(int* bad) {
 // is taken between the two nearby pairs; the cells then follow by widths.
 //
 // Cells are read through records rec[d] = (db_hi[d], db_lo[d], w[d],
-// db_hi[d+1]) and sinogram planes q[qd][d][QW] with plane stride qs; `rec` and
+// w[d+1]) and sinogram planes q[qd][d][QW] with plane stride qs; `rec` and
 // `q` point at cell `base`; the search stays in [dlo, dhi), and the straight-
 // line steps read at most two padding cells past it. The same code runs on a
 // shared-memory window of the cells (SM, seeded per tile) and on the global
@@ -723,24 +727,29 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
   // The cell: db_hi[d] <= xs < db_hi[d+1], d in [dlo, dhi), then one cell back
   // if the offset of the edge into it, taken between the two nearby pairs, is
   // negative. The seed is almost always that cell with a non-negative offset,
-  // which one test confirms; otherwise the search walks from the seed.
+  // which one test confirms (conservatively: an edge within ub_margin of the
+  // upper boundary takes the search); otherwise the search walks from the seed.
+  // A record carries the next cell's width (w1) instead of its boundary.
   int d = seed_cell(P.scan, (float)xs, sd, dlo, dhi);
   Quad<T> rd = ldrec<T, SM>(rec + (d - base) * 4);
-  T a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
-  T w0 = rd.z;
-  if (!(rd.x <= xs && xs < rd.w && a >= T(0))) {
+  const T off = sub_rn(xs, rd.x);
+  T a = add_rn(off, sub_rn(xl, rd.y));
+  T w0 = rd.z, w1 = rd.w;
+  if (!(rd.x <= xs && off < rd.z - P.ub_margin && a >= T(0))) {
     while (d > dlo && xs < rd.x) {
       --d;
       rd = ldrec<T, SM>(rec + (d - base) * 4);
     }
-    while (d < dhi - 1 && rd.w <= xs) {  // after a step down, rd.w > xs already
+    while (d < dhi - 1 && rec[(d + 1 - base) * 4] <= xs) {  // db_hi[d+1]; none after a step down
       ++d;
       rd = ldrec<T, SM>(rec + (d - base) * 4);
     }
     a = add_rn(sub_rn(xs, rd.x), sub_rn(xl, rd.y));
     w0 = rd.z;
+    w1 = rd.w;
     if (a < T(0) && d > dlo) {
       --d;
+      w1 = w0;
       w0 = rec[(d - base) * 4 + 2];
       a += w0;
     }
@@ -761,7 +770,7 @@ __device__ __forceinline__ void pix_geom(const DevPlan<T>& P, const Quad<T>& A4,
 #pragma unroll
   for (int j = 0; j < U; ++j) {
     cs.oj[j] = d + j - base;
-    const T w = j == 0 ? w0 : rec[cs.oj[j] * 4 + 2];
+    const T w = j == 0 ? w0 : (j == 1 ? w1 : rec[cs.oj[j] * 4 + 2]);
     const T ov = fmax(fmin(b, w) - fmax(a, T(0)), T(0));
     cs.ov[j] = KIND == kB ? ov * wv : ov;
     a -= w;
@@ -1519,7 +1528,7 @@ static int upload(ctgb_plan* p) {
       e[0] = db2[2 * b];
       e[1] = db2[2 * b + 1];
       e[2] = g.wd[(size_t)v * D + d];
-      e[3] = db2[2 * b + 2];
+      e[3] = d + 1 < D ? g.wd[(size_t)v * D + d + 1] : 0.0;  // the padding cell's width past D
     }
   for (size_t i = 0; i < (size_t)V * L; ++i) {
     const double alpha = g.lp[2 * i], sigma = g.lp[2 * i + 1];
@@ -1572,6 +1581,12 @@ static int upload(ctgb_plan* p) {
   DevPlan<T> P{};
   P.V = V; P.D = D; P.W = g.W; P.H = g.H; P.L = L; P.scan = g.scan;
   P.dImg = (T)g.dImg; P.s2r = (T)g.s2r; P.dAng = (T)g.dAng; P.wscale = (T)g.wscale;
+  {
+    double m = 0.0;
+    for (const double x : g.db) m = std::max(m, std::fabs(x));
+    for (const double x : g.wd) m = std::max(m, std::fabs(x));
+    P.ub_margin = (T)std::ldexp(4.0, std::ilogb(m) + 1 - std::numeric_limits<T>::digits);
+  }
   P.wsrc = reinterpret_cast<const T*>(b + offs[0]);
   P.db2 = reinterpret_cast<const T*>(b + offs[1]);
   P.wd = reinterpret_cast<const T*>(b + offs[2]);
