@@ -7,13 +7,15 @@
 //   detector gather (A, B^T): one thread per (view, detector cell) walks all
 //     image lines of its view; per line it maps its two cell boundaries into
 //     pixel-edge coordinates (one FMA each) and sums the 1-3 overlapped pixels.
-//     A CTA is 8 consecutive views x 32 consecutive cells, so the 8 warps read
-//     nearly the same pixels of the same line and share them through L1.
-//   image gather (A^T, B): one thread per pixel walks all views; per view it
-//     maps its two pixel edges onto the axis, seeds the detector cell from a
-//     closed-form inverse of the boundary map, corrects it against the stored
-//     boundaries and sums the 1-3 overlapped cells. A CTA is a 32 x 8 pixel
-//     tile, whose footprint per view is ~40 consecutive cells.
+//     A CTA is 4 or 8 consecutive views x 32 consecutive cells, so its warps
+//     read nearly the same pixels of the same line and share them through L1.
+//   image gather (A^T, B): one thread per pixel (or 2-4 pixel rows) walks all
+//     views; per view it maps its lower pixel edge onto the axis, seeds the
+//     detector cell (a per-tile quadratic of the closed-form inverse of the
+//     boundary map), confirms or corrects it against the stored boundaries and
+//     sums the 1-3 overlapped cells. A CTA is a 32-column pixel tile whose
+//     footprint per view is a few dozen consecutive cells, staged by a producer
+//     warp into a shared-memory ring with TMA bulk copies.
 //
 // Slices are processed SB at a time per thread (geometry computed once, SB
 // fused multiply-adds per overlap); inputs are first re-laid out so that the
@@ -626,10 +628,11 @@ __device__ __forceinline__ void report_timeout(int* bad) {
 // image gather: A^T (kind kAt) and B (kind kB)
 // ----------------------------------------------------------------------------
 // Thread = pixel (r, c), SB slices, loop over views. Per view the pixel's lower
-// edge x = alpha + sigma*k is formed as an unevaluated pair (two-product and
-// two-sum), its cell d is seeded from the closed-form inverse of the boundary
-// map and corrected against the stored boundaries, and the offset a = x - db[d]
-// is taken between the two nearby pairs; the cells then follow by widths.
+// edge x = alpha + sigma*k is formed as an unevaluated pair (an exact high part
+// from grid-aligned line maps, and a low part), its cell d is seeded and
+// confirmed (or corrected) against the stored boundaries, and the offset
+// a = x - db[d] is taken between the two nearby pairs; the cells then follow by
+// widths.
 //
 // Cells are read through records rec[d] = (db_hi[d], db_lo[d], w[d],
 // w[d+1]) and sinogram planes q[qd][d][QW] with plane stride qs; `rec` and
