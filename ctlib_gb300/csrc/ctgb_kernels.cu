@@ -1512,6 +1512,24 @@ struct ctgb_plan {
 
 namespace ctgb {
 
+// Line map x(k) = alpha + sigma*k of a line with K pixels, split for a type of
+// `digits` significant bits into (alpha_hi, alpha_lo, sigma_hi, sigma_lo). The
+// high parts are rounded to multiples of one power of two qg, chosen so that
+// every value alpha_hi + sigma_hi*k (k = 0 .. K, the line's pixel edges) is a
+// multiple of qg below 2^digits qg in magnitude: that sum is then exact in the
+// type and the image gather forms it with one FMA. The low parts are the
+// remainders (at most qg/2 each), summed by a second FMA to ~2^-38 of the
+// coordinate in fp32. The device table stores each part rounded to the type.
+static void split_line_map(double alpha, double sigma, int K, int digits, double* out) {
+  const double M = std::max({std::fabs(alpha), std::fabs(alpha + sigma * K), sigma * K});
+  const double qg = std::ldexp(1.0, std::ilogb(M) + 2 - digits);
+  const double ah = std::nearbyint(alpha / qg) * qg, sh = std::nearbyint(sigma / qg) * qg;
+  out[0] = ah;
+  out[1] = alpha - ah;
+  out[2] = sh;
+  out[3] = sigma - sh;
+}
+
 template <class T>
 static int upload(ctgb_plan* p) {
   const HostGeom& g = p->geom;
@@ -1543,18 +1561,7 @@ static int upload(ctgb_plan* p) {
     const double gh = split_hi(gam), bi = std::floor(beta);
     lg[4 * i] = gh; lg[4 * i + 1] = gam - gh; lg[4 * i + 2] = bi; lg[4 * i + 3] = beta - bi;
     ls[i] = sigma;
-    // Line map x(k) = alpha + sigma*k. The high parts are rounded to multiples
-    // of one power of two qg, chosen so that every value alpha_hi + sigma_hi*k
-    // (k = 0 .. K, the line's pixel edges) is a multiple of qg below 2^p qg in
-    // magnitude, p the precision of T: that sum is then exact in T and the
-    // image gather forms it with one FMA. The low parts are the remainders
-    // (at most qg/2 each), summed by a second FMA to ~2^-38 of the coordinate
-    // in fp32.
-    const int K = (g.flags[i / L] & 1) ? g.W : g.H;
-    const double M = std::max({std::fabs(alpha), std::fabs(alpha + sigma * K), sigma * K});
-    const double qg = std::ldexp(1.0, std::ilogb(M) + 2 - std::numeric_limits<T>::digits);
-    const double ah = std::nearbyint(alpha / qg) * qg, sh = std::nearbyint(sigma / qg) * qg;
-    lp[4 * i] = ah; lp[4 * i + 1] = alpha - ah; lp[4 * i + 2] = sh; lp[4 * i + 3] = sigma - sh;
+    split_line_map(alpha, sigma, (g.flags[i / L] & 1) ? g.W : g.H, std::numeric_limits<T>::digits, &lp[4 * i]);
   }
   for (int r = 0; r < g.H; ++r) rowc[r] = (g.height / 2 - r - 0.5) * g.dImg;
   for (int c = 0; c < g.W; ++c) colc[c] = (c - g.width / 2 + 0.5) * g.dImg;
@@ -2657,6 +2664,19 @@ long ctgb_geometry_query(const double* options, int n_options, int dtype, int wh
     return -1;
   }
   std::vector<double> flags(g.flags.begin(), g.flags.end());
+  std::vector<double> split;
+  if (what == 7) {  // the image gather's line maps as the device stores them
+    const int L = g.L;
+    split.assign((size_t)g.V * L * 4, 0.0);
+    for (size_t i = 0; i < (size_t)g.V * L; ++i) {
+      const double alpha = g.lp[2 * i], sigma = g.lp[2 * i + 1];
+      if (!(sigma > 0)) continue;
+      double* o = &split[4 * i];
+      ctgb::split_line_map(alpha, sigma, (g.flags[i / L] & 1) ? g.W : g.H, dtype == 0 ? 24 : 53, o);
+      if (dtype == 0)
+        for (int j = 0; j < 4; ++j) o[j] = (double)(float)o[j];
+    }
+  }
   const std::vector<double>* src = nullptr;
   switch (what) {
     case 0: src = &flags; break;
@@ -2666,6 +2686,7 @@ long ctgb_geometry_query(const double* options, int n_options, int dtype, int wh
     case 4: src = &g.inv; break;
     case 5: src = &g.wpre; break;
     case 6: src = &g.taps; break;
+    case 7: src = &split; break;
     default: ctgb::fail(CTGB_ERR_INVALID, "unknown geometry table"); return -1;
   }
   if (out) {

@@ -256,7 +256,10 @@ int ctgb_version(void);
  * and tooling). `what`: 0 flags (V ints as doubles: bit0 row lines, bit1
  * flipped), 1 detector boundaries (V*(D+1)), 2 A/A^T factors (V*D),
  * 3 line maps (V*L*2: alpha, sigma), 4 inverse seeds (V*5), 5 fbp pre-weight (D),
- * 6 ramp taps (2D-1). Returns the element count, or -1 on error. */
+ * 6 ramp taps (2D-1), 7 the image gather's split line maps as stored for `dtype`
+ * (V*L*4: alpha hi, alpha lo, sigma hi, sigma lo, each rounded to the type; the
+ * high parts make alpha_hi + sigma_hi*k exact for every pixel edge k of the
+ * line). Returns the element count, or -1 on error. */
 long ctgb_geometry_query(const double* options, int n_options, int dtype, int what, double* out,
                          size_t n_out);
 

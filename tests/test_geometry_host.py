@@ -139,3 +139,43 @@ def test_fbp_tables_match_reference_taps(native, oracle_mod):
         dt = 0 if z["ramp_taps"].dtype == np.float32 else 1
         taps = _query(native, list(z["options"]), 6, dtype=dt)
         assert np.array_equal(taps.astype(z["ramp_taps"].dtype), z["ramp_taps"]), f
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("opts", CASES)
+def test_split_line_maps_exact_high_part(native, opts, dtype):
+    """The image gather forms a pixel edge as (fma(sigma_hi, k, alpha_hi),
+    fma(sigma_lo, k, alpha_lo)): the high parts lie on one power-of-two grid per
+    line, so alpha_hi + sigma_hi * k is exact in the plan's type for every edge k
+    of the line, and the pair sums to alpha + sigma * k to the type's precision
+    (checked on up to 16 views of each case, every line)."""
+    V, D, W, H = (int(opts[i]) for i in range(4))
+    L = max(W, H)
+    lp = _query(native, opts, 3, dtype=dtype).reshape(V, L, 2)  # the plan's own geometry
+    sp = _query(native, opts, 7, dtype=dtype).reshape(V, L, 4)
+    flags = _query(native, opts, 0).astype(int)
+    bits = 24 if dtype == 0 else 53
+    for v in range(0, V, max(1, V // 16)):
+        K = W if flags[v] & 1 else H
+        used = lp[v, :, 1] > 0
+        alpha, sigma = lp[v, used, 0], lp[v, used, 1]
+        ah, al, sh, sl = (sp[v, used, j] for j in range(4))
+        if dtype == 0:
+            for x in (ah, al, sh, sl):
+                assert np.array_equal(x.astype(np.float32).astype(np.float64), x)
+        # the grid: 2^(exponent of the line's largest edge magnitude + 2 - bits)
+        M = np.maximum.reduce([np.abs(alpha), np.abs(alpha + sigma * K), sigma * K])
+        q = np.ldexp(1.0, np.frexp(M)[1] + 1 - bits)
+        A, S = ah / q, sh / q
+        assert np.array_equal(A, np.round(A)) and np.array_equal(S, np.round(S))
+        A, S = A.astype(np.int64), S.astype(np.int64)
+        edge_hi_max = np.maximum(np.abs(A), np.abs(A + S * K))  # alpha_hi + sigma_hi k is monotone in k
+        assert (edge_hi_max < 2 ** bits).all()  # every edge's high part is exact
+        k = np.arange(K + 1)[None, :]
+        got = (ah[:, None] + sh[:, None] * k) + (al[:, None] + sl[:, None] * k)
+        want = alpha[:, None] + sigma[:, None] * k
+        scale = np.abs(want).max(axis=1) + sigma
+        # fp32: the low parts carry the edge to ~2^-38; fp64: the check itself
+        # rounds in double (a few units in the last place)
+        tol = 2.0 ** -36 if dtype == 0 else 2.0 ** -50
+        assert (np.abs(got - want).max(axis=1) <= tol * scale).all(), v
