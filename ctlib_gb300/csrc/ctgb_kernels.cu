@@ -897,12 +897,13 @@ struct PixSlot {
   static constexpr int kBytes = kQBytes + kRecBytes + kLpBytes;
 };
 
-// CTAs per SM of the staged image gather: four at one fp32 slice per thread,
-// whose sums fit 56 registers and whose small slots leave room for four CTAs'
-// rings (more warps to hide the shared-memory latency of an issue-bound loop);
-// three otherwise (72 registers).
+// CTAs per SM of the staged image gather: four at one to four fp32 slices per
+// thread, whose sums fit 56 registers and whose small slots leave room for four
+// CTAs' rings (more warps to hide the shared-memory latency of an issue-bound
+// loop; A^T of 2 and 4 512^2 slices: 1.05 -> 0.88 and 1.13 -> 1.05 ms); three
+// otherwise (72 registers).
 template <class T, int SB>
-constexpr int kPixCtas = (sizeof(T) == 4 && SB == 1) ? 4 : 3;
+constexpr int kPixCtas = (sizeof(T) == 4 && SB <= 4) ? 4 : 3;
 
 // Views in flight per CTA: as many slots as fit beside the Kahan sums of 8 row
 // warps with kPixCtas CTAs per SM (228 KB of shared memory per SM, less 2 KB per
@@ -1735,13 +1736,13 @@ template <class T, int SB, int PX>
 static int launch_pix_rows(const ctgb_plan* p, const DevPlan<T>& P, int op, int sched, T* y, int batch, const T* qb,
                            T* parts, int nsplit, cudaStream_t st);
 
-// Four pixel rows per consumer thread are built for one fp32 slice per thread:
-// they share each warp's per-view costs between twice the pixels of two rows,
-// and are taken when the grid still fills two waves (16 x 16 tiles x 8 view
-// parts for one 512^2 slice of 1152 views: A^T 0.97 -> 0.85 ms), not on small
-// images (parallel 256^2, 360 views: 128 CTAs, 0.14 -> 0.18 ms).
+// Four pixel rows per consumer thread are built for one or two fp32 slices per
+// thread: they share each warp's per-view costs between twice the pixels of
+// two rows, and are taken when the grid still fills two waves (16 x 16 tiles x
+// 8 view parts for one 512^2 slice of 1152 views: A^T 0.97 -> 0.85 ms), not on
+// small images (parallel 256^2, 360 views: 128 CTAs, 0.14 -> 0.18 ms).
 template <class T, int SB>
-constexpr bool kWideBuilt = sizeof(T) == 4 && SB == 1;
+constexpr bool kWideBuilt = sizeof(T) == 4 && SB <= 2;
 
 // Staged image gather (A^T, B, fbp's backprojection, single-view B) from the
 // sinogram planes qb; unless `planes_ready`, qb is first filled from x (re-layout,
