@@ -910,8 +910,9 @@ constexpr int kPixCtas = (sizeof(T) == 4 && SB <= 4) ? 4 : 3;
 // CTA for the static arrays and the per-CTA reserve: 74 KB of dynamic shared
 // memory each at three CTAs, 55 KB at four), at most 16. The ring has to cover
 // the time from a slot's release by the slowest row warp to its refill
-// landing; the few-slice slots are small, so those rings get deep (16 slots
-// for one to four slices per thread, 11 for eight, 7 for sixteen).
+// landing; the few-slice slots are small, so those rings get deep (fp32: 16
+// slots for one slice per thread, 15 with four pixel rows; 13 and 10 for two
+// slices; 15 for four, 11 for eight, 7 for sixteen).
 template <class T, int SB, int PX = kPixRows<SB>>
 constexpr int kSlots = [] {
   constexpr int acc = 2 * PX * SB * 256 * (int)sizeof(T);
